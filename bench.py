@@ -1,0 +1,317 @@
+"""Benchmark: time to relative residual 1e-8 on the 128^3 graph Laplacian with IC(0).
+
+Workload (one "step" = one full solve from x0 = 0):
+  128^3 7-point Laplacian, edge weights lognormal(0, 0.5), + 1e-3 I (n = 2,097,152,
+  nnz = 14,581,760), b ~ U[-1,1] (seed 1002), IC(0), tol 1e-8 relative to ||b||.
+  value  = mixed precision (FP32 inner PCG, FP64 iterative refinement) solve time,
+           device-resident inputs, CUDA events on the solver stream;
+  fp64   = the plain FP64 device PCG on the same system (the comparator the
+           metric names);
+  e2e    = the same mixed solve through gb_pcg_solve_host from pinned host
+           buffers (b, x0 in; x out), copies inside the timed region.
+Inputs (matrix 175 MB FP64 + 117 MB FP32 copy + factors) exceed the 129 MB L2,
+so no explicit L2 flush is done between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's CPU algorithm (the oracle's C
+restatement, multithreaded SpMV/dot as LAP's OpenMP backend) on this host on a
+bounded sample of iterations, scaled to the full iteration count.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time to rel-res 1e-8, mixed-prec IC0-PCG on 128^3 Laplacian (1 GB300)"
+UNIT = "ms"
+WORKLOAD = "grid3d_lognormal_128 (n=2097152, nnz=14581760), IC0, tol 1e-8"
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of each kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows: list[list[str]] = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 9
+                          for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allmax(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_workload(nside):
+    from lap_gb300 import gen
+
+    return gen.grid3d_lognormal(nside, seed=1002)
+
+
+def cpu_baseline(A, b, full_iters, target_s=12.0, kind="serial"):
+    """The oracle (our C restatement of LAP's CPU PCG) on a bounded sample."""
+    import oracle
+
+    probe = oracle.solve(A.n, A.ia, A.ja, A.a, b, "ichol", 1e-8, 100000, kind=kind, max_iters_run=3)
+    per_it = probe["solve_s"] / max(probe["iters"], 1)
+    m = int(max(3, min(full_iters, target_s / max(per_it, 1e-6))))
+    r = oracle.solve(A.n, A.ia, A.ja, A.a, b, "ichol", 1e-8, 100000, kind=kind, max_iters_run=m)
+    per_it = r["solve_s"] / max(r["iters"], 1)
+    return dict(value=per_it * full_iters * 1e3, unit=UNIT, cores=oracle.lib(kind).orc_num_threads(),
+                kind="port", sample=f"{r['iters']} of {full_iters} IC0-PCG iterations (FP64, CPU) on "
+                f"the full 128^3 matrix, {per_it * 1e3:.1f} ms/iteration, scaled to the full solve; "
+                f"IC0 setup {r['setup_s']:.1f} s excluded as LAP's Time line excludes it")
+
+
+def run_reference(args, world, rank):
+    """The reference's CPU PCG (oracle restatement, OpenMP mirror) timed on host cores."""
+    if rank != 0:
+        return
+    import oracle
+
+    A, b = make_workload(args.size)
+    t0 = time.time()
+    full = oracle.solve(A.n, A.ia, A.ja, A.a, b, "ichol", 1e-8, 100000, kind="omp")
+    iters = full["iters"]
+    m = max(2, min(iters, args.sample_iters))
+    times = []
+    for s in range(args.warmup + args.steps):
+        r = oracle.solve(A.n, A.ia, A.ja, A.a, b, "ichol", 1e-8, 100000, kind="omp", max_iters_run=m)
+        if s >= args.warmup:
+            times.append(r["solve_s"] / r["iters"] * iters * 1e3)
+    v = statistics.mean(times)
+    cores = oracle.lib("omp").orc_num_threads()
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD + " (reference: FP64 IC0-PCG, CPU)", "iterations": iters,
+                       "sample_iterations": m},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{m} of {iters} IC0-PCG iterations per step on the full "
+                                       f"matrix, scaled to the full solve; LAP OpenMP backend "
+                                       f"mirror (SpMV/dot on {cores} threads, serial triangular "
+                                       f"solves)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": time.time() - t0}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    import lap_gb300 as gb
+
+    torch.cuda.set_device(local)
+    A, b = make_workload(args.size)
+    n, nnz = A.n, A.nnz
+    sysm = gb.System.from_csr(A, "ichol")
+    info = sysm.info()
+    db = torch.from_numpy(b).cuda()
+    kw = dict(tol=args.tol, maxit=20000)
+
+    # warm-up: graphs captured, clocks up
+    for _ in range(args.warmup):
+        sysm.solve(db, precision=1, **kw)
+        sysm.solve(db, precision=0, **kw)
+
+    def timed(precision, steps):
+        ms, res = [], None
+        barrier(world)
+        torch.cuda.synchronize()
+        for _ in range(steps):
+            x, res = sysm.solve(db, precision=precision, **kw)
+            ms.append(res["device_ms"])
+        torch.cuda.synchronize()
+        barrier(world)
+        return ms, res, x
+
+    with ClockSampler(local) as clk:
+        t0 = time.time()
+        ms_mixed, r_mixed, x_mixed = timed(1, args.steps)
+        wall = time.time() - t0
+    ms_fp64, r_fp64, x_fp64 = timed(0, max(2, args.steps // 2))
+
+    # end to end from pinned host buffers
+    bh = torch.from_numpy(b).pin_memory()
+    xh = torch.zeros(n, dtype=torch.float64).pin_memory()
+    e2e = []
+    for _ in range(args.steps):
+        xh.zero_()
+        r = gb.PcgResult()
+        o = gb.opts(precision=1, **kw)
+        gb.check(gb.lib().gb_pcg_solve_host(sysm.h, bh.data_ptr(), xh.data_ptr(), gb.C.byref(o),
+                                            gb.C.byref(r)), "gb_pcg_solve_host")
+        e2e.append(r.device_ms)
+
+    # per-kernel device time of one iteration (CUDA events on the solver stream)
+    peak, peak_kind = measured_peak()
+    prof = {p: sysm.profile(db, precision=p, iters=20) for p in (0, 1)}
+    traffic = ncu_traffic()
+    kernels = []
+    for p, lst in prof.items():
+        for k in lst:
+            gbs = k["bytes"] / (k["ms"] * 1e-3) / 1e9 if k["ms"] > 0 else 0.0
+            kernels.append({"kernel": k["name"], "precision": "mixed-fp32" if p else "fp64",
+                            "ms": round(k["ms"], 5), "bytes": k["bytes"], "gbs": round(gbs, 1),
+                            "frac": round(gbs / peak, 4)})
+    mixed_k = [k for k in kernels if k["precision"] == "mixed-fp32"]
+    dom = max(mixed_k, key=lambda k: k["ms"])
+    tr = traffic.get(f"{dom['kernel']}:{dom['precision']}")
+    roofline = {"bound": "hbm", "kernel": dom["kernel"], "achieved": dom["gbs"], "peak": peak,
+                "unit": "GB/s", "frac": dom["frac"], "traffic": tr,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s"}
+
+    v = allmax(world, statistics.mean(ms_mixed))
+    v64 = allmax(world, statistics.mean(ms_fp64))
+    ve2e = allmax(world, statistics.mean(e2e))
+    if rank != 0:
+        return
+    it_in, outer = r_mixed["iters"], r_mixed["outer"]
+    # kernels per solve: FP64 = prologue 3 + 3/iteration (+ the final no-op body) + true residual;
+    # mixed = per refinement step (outer residual + prologue 3 + 3/iteration + correction)
+    launches_mixed = it_in * 3 + outer * (1 + 3 + 3 + 1) + 1 + 1
+    line = {"metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v, 4),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 inner / f64 refinement", "data": "synthetic (seeded generator, no dataset)",
+            "config": {"workload": WORKLOAD, "n": n, "nnz": nnz, "preconditioner": "ichol",
+                       "precision": "FP32 inner PCG + FP64 iterative refinement",
+                       "l2": "inputs larger than L2 (no flush)",
+                       "lower_levels": info["lower_levels"], "upper_levels": info["upper_levels"],
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "mixed": {"ms": round(v, 4), "inner_iters": it_in, "outer": outer,
+                      "rel_true_res": r_mixed["rel_true_res"]},
+            "fp64": {"ms": round(v64, 4), "iters": r_fp64["iters"], "rel_true_res": r_fp64["rel_true_res"]},
+            "speedup_mixed_vs_fp64": round(v64 / v, 3),
+            "solves_per_s_all_gpus": round(world * 1e3 / v, 3),
+            "e2e": {"value": round(ve2e, 4), "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * n,
+                    "d2h_bytes_per_step": 8 * n},
+            "roofline": roofline, "kernels": kernels,
+            "gpu_launches": launches_mixed * args.steps,
+            "clocks": clk.summary(), "wall_s_timed": round(wall, 3)}
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(A, b, r_fp64["iters"])
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--size", type=int, default=128)
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--sample-iters", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        import __graft_entry__
+
+        __graft_entry__.build() if not os.path.exists(os.path.join(ROOT, "lap_gb300", "libgblap.so")) else None
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

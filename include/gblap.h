@@ -1,0 +1,173 @@
+/*
+ * gblap.h -- device-resident extended API of libgblap.so (sm_103a).
+ *
+ * LAP itself has no such layer: its cg() (cg.c:5-140) drives every BLAS call
+ * from the host and synchronises three times per iteration.  This API keeps
+ * the whole PCG loop on the GPU (fused kernels, device-side convergence
+ * test, one CUDA-graph launch per solve) and adds mixed precision, batching
+ * and an adjoint.  Plain pointers and sizes only; every array is a DEVICE
+ * pointer unless its name ends in _host.  Every function returns a
+ * gb_status; results that LAP reports through cg()'s `flag` keep that
+ * meaning in gb_pcg_result.flag.
+ */
+#ifndef GBLAP_H
+#define GBLAP_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GB_OK = 0,
+  GB_MAXIT = 1,        /* more than maxit iterations (cg.c:119) */
+  GB_BREAKDOWN = 2,    /* p'q <= 0 or a non-finite scalar in the recurrence */
+  GB_ZERO_PIVOT = 3,   /* IC(0) met a non-positive pivot */
+  GB_TIMEOUT = 4,      /* a sync-free wait exceeded its time limit */
+  GB_BAD_INPUT = 5,    /* malformed CSR, missing diagonal, bad sizes, unknown name */
+  GB_CUDA_ERROR = 6,
+  GB_NO_MEMORY = 7,
+  GB_NOT_SUPPORTED = 8
+} gb_status;
+
+/* Preconditioner names are LAP's (prec.c:6-45). */
+typedef enum {
+  GB_PREC_NONE = 0,        /* "none"        */
+  GB_PREC_LINE_JACOBI = 1, /* "line_jacobi" : y = D^-1 x (line_jacobi.c:3-7) */
+  GB_PREC_IT_JACOBI = 2,   /* "it_jacobi"   : k Jacobi sweeps (it_jacobi.c:4-33) */
+  GB_PREC_GS_STD = 3,      /* "GS_std"      : k forward + k backward GS sweeps (GS.c:5-42) */
+  GB_PREC_GS_IT = 4,       /* "GS_it"       : GS.c:45-92 */
+  GB_PREC_GS_IT2 = 5,      /* "GS_it2"      : GS.c:95-159 */
+  GB_PREC_ICHOL = 6        /* "ichol"       : IC(0) on A's pattern (simple_blas.c:139-223) */
+} gb_prec;
+
+const char *gb_status_str(int status);
+/* Maps a LAP preconditioner name to gb_prec; returns -1 for an unknown name. */
+int gb_prec_from_name(const char *name);
+/* Library build string (arch, version). */
+const char *gb_version(void);
+
+/* ------------------------------------------------------------ solver object */
+typedef struct gb_system_s *gb_system;
+
+/* Wraps a device CSR matrix (full symmetric pattern, 0-based int32 indices,
+ * columns ascending, no duplicates, every diagonal stored).  The arrays are
+ * borrowed and must outlive the object.  Builds the SpMV row tiling, the
+ * level schedules of the triangular factors and, for "ichol", the IC(0)
+ * factor on the device.  m, k are LAP's M (outer) and K (inner) counts. */
+int gb_system_create(int n, int nnz, const int *ia, const int *ja, const double *a,
+                     const char *prec_name, int m, int k, gb_system *out);
+int gb_system_destroy(gb_system sys);
+/* Re-reads the matrix values (same pattern) and refactors / refreshes the
+ * preconditioner and the FP32 copies. */
+int gb_system_update_values(gb_system sys);
+/* Levels of the lower / upper sync-free schedules and SpMV tiles (diagnostics). */
+int gb_system_info(gb_system sys, int *lower_levels, int *upper_levels, int *spmv_tiles);
+
+typedef struct {
+  double tol;        /* stop when ||r|| < tol*||r0|| (cg.c:60,107); mixed: ||b-Ax|| < tol*||b-Ax0|| */
+  int maxit;         /* iteration cap; like cg.c at most maxit+1 iterations run */
+  int precision;     /* 0: FP64 PCG.  1: FP32 inner PCG inside FP64 iterative refinement */
+  double inner_tol;  /* mixed: residual reduction asked of each inner solve (default 1e-4) */
+  int max_outer;     /* mixed: refinement steps cap (default 50) */
+  int use_graph;     /* 1 (default): the iteration loop is one CUDA graph with a device-side
+                        while node; 0: host-launched kernels, one status read per 16 iterations */
+  int verbose;       /* print LAP's per-iteration line "CG: it %d, res norm %5.5e" */
+} gb_pcg_opts;
+
+typedef struct {
+  int iters;           /* PCG iterations (mixed: sum over refinement steps) */
+  int outer;           /* refinement steps (mixed), 0 for FP64 */
+  int flag;            /* cg.c: 0 converged, 1 maxit, 2 failure */
+  int status;          /* gb_status */
+  double res0;         /* ||b - A x0|| */
+  double res;          /* final recursive residual norm (FP64 true residual for mixed) */
+  double true_res;     /* ||b - A x|| recomputed in FP64 after the solve */
+  double rel_true_res; /* true_res / ||b|| (the quantity cg.c:117 prints) */
+  double device_ms;    /* device time of the solve, CUDA events on the system stream */
+} gb_pcg_result;
+
+void gb_pcg_opts_default(gb_pcg_opts *opts);
+
+/* Solves A x = b.  x holds x0 on entry.  res_hist_host (may be NULL) receives
+ * up to hist_len residual norms, res_hist_host[0] = ||r0|| as cg.c.  Blocks
+ * until the solve is complete. */
+int gb_pcg_solve(gb_system sys, const double *b, double *x, const gb_pcg_opts *opts,
+                 double *res_hist_host, int hist_len, gb_pcg_result *result);
+
+/* Same solve, from and to HOST buffers (b_host, x_host of n doubles; x_host
+ * holds x0).  The host<->device copies are part of the call. */
+int gb_pcg_solve_host(gb_system sys, const double *b_host, double *x_host,
+                      const gb_pcg_opts *opts, gb_pcg_result *result);
+
+/* ------------------------------------------------------------ kernels */
+/* y = alpha*A*x + beta*y (FP64), LAP's row-sequential summation order. */
+int gb_spmv(gb_system sys, double alpha, const double *x, double beta, double *y);
+/* y = M^{-1} x with the system's preconditioner (prec_function semantics). */
+int gb_precond_apply(gb_system sys, const double *x, double *y);
+/* IC(0) factor values in LAP's CPU layout: L (diagonal last per row, strict
+ * lower pattern + diagonal) and U = L^T (diagonal first), each nnz_lower+n
+ * doubles, device pointers. */
+int gb_ichol_factor_values(gb_system sys, double *l_vals, double *u_vals);
+
+/* ------------------------------------------------------------ adjoint */
+/* Given the solution x of A x = b and the adjoint lambda of A lambda = g,
+ * writes G[k] = -lambda[i] * x[j] for every stored entry k = (i, j) of A
+ * (dL/dA on A's pattern) and, when edge_grad is non-NULL, for every entry of
+ * the strict lower triangle in row-major order the edge-weight gradient
+ * dL/dw_ij = G_ij + G_ji - G_ii - G_jj = -(lambda_i - lambda_j)(x_i - x_j)
+ * for a Laplacian A = L(w) + shift. */
+int gb_adjoint_scatter(gb_system sys, const double *x, const double *lambda, double *G,
+                       double *edge_grad);
+/* Full adjoint step: solves A lambda = g with the same PCG (A is SPD) and
+ * scatters.  dL/db = lambda. */
+int gb_adjoint_grad(gb_system sys, const double *x, const double *g, double *lambda,
+                    double *G, double *edge_grad, const gb_pcg_opts *opts,
+                    gb_pcg_result *result);
+
+/* ------------------------------------------------------------ batching */
+typedef struct gb_batch_s *gb_batch;
+/* count independent CSR systems concatenated block-diagonally: row_off[count+1]
+ * and nnz_off[count+1] (host, int64) give each system's rows / entries in the
+ * concatenated ia (local 0-based row pointers per system, each starting at 0),
+ * ja (local column indices) and a arrays.  Preconditioner: "line_jacobi". */
+int gb_batch_create(int count, const long long *row_off_host, const long long *nnz_off_host,
+                    const int *ia, const int *ja, const double *a, const char *prec_name,
+                    gb_batch *out);
+int gb_batch_destroy(gb_batch batch);
+/* Solves every system; b, x concatenated.  iters_host / flags_host (may be
+ * NULL) receive per-system iteration counts and cg.c flags.  The tile and
+ * row-bundle shape is chosen by the autotuner on first use. */
+int gb_batch_solve(gb_batch batch, const double *b, double *x, const gb_pcg_opts *opts,
+                   int *iters_host, int *flags_host, gb_pcg_result *result);
+
+/* Multi-RHS: nrhs right-hand sides on one system, b and x row-major
+ * [nrhs][n].  Each column runs its own PCG recurrence; the matrix is read
+ * once per iteration for all columns. */
+int gb_pcg_solve_multi(gb_system sys, int nrhs, const double *B, double *X,
+                       const gb_pcg_opts *opts, int *iters_host, gb_pcg_result *result);
+
+/* ------------------------------------------------------------ autotuner */
+/* Times the SpMV variants on this system and keeps the fastest (cached per
+ * matrix shape class).  best_host receives the chosen rows-per-bundle. */
+int gb_autotune_spmv(gb_system sys, int *best_host);
+
+/* ------------------------------------------------------------ failure injection */
+/* Test hook: wall-clock limit (ns) of every sync-free wait in this system's
+ * solves and factorization; 0 restores the default of one second.  A wait
+ * that runs out records GB_TIMEOUT, releases its dependents with a NaN and
+ * returns, so the solve ends with status GB_TIMEOUT instead of hanging. */
+int gb_debug_set_spin_budget(gb_system sys, unsigned long long ns);
+
+/* ------------------------------------------------------------ measurement */
+/* Per-kernel device times (ms per launch, CUDA events on the system stream)
+ * of one PCG iteration's kernels, averaged over `iters` iterations run
+ * eagerly.  names_host receives a ';'-separated list of kernel names,
+ * ms_host[i] and bytes_host[i] the average time and algorithmic bytes. */
+int gb_profile_iteration(gb_system sys, const double *b, double *x, int precision, int iters,
+                         char *names_host, int names_len, double *ms_host,
+                         double *bytes_host, int max_kernels, int *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

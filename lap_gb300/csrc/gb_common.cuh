@@ -1,0 +1,197 @@
+// gb_common.cuh -- shared device helpers for libgblap (sm_103a).
+//
+// * deterministic block / grid reductions (last-block ticket, fixed order);
+// * relaxed/acquire/release global accesses for the sync-free solvers;
+// * "not yet computed" sentinels: a sync-free triangular solve pre-fills its
+//   output with a signalling-NaN bit pattern and every consumer spins on the
+//   value itself, so one 8-byte load carries both readiness and data.  IEEE
+//   arithmetic never produces a signalling NaN, and a computed value that
+//   happens to equal the pattern is rewritten to a quiet NaN before storing.
+// * every spin has a wall-clock limit (globaltimer): on expiry the waiter
+//   sets the error word, and consumers stop waiting once it is set.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gblap_internal.h"
+
+#define GB_WARP 32
+
+namespace gb {
+
+// --------------------------------------------------------------- sentinels
+__device__ __forceinline__ double sentinel_f64() {
+  return __longlong_as_double(0x7FF4DEADBEEF0001LL);
+}
+__device__ __forceinline__ float sentinel_f32() { return __int_as_float(0x7FA0DEAD); }
+__device__ __forceinline__ bool is_sentinel(double v) {
+  return __double_as_longlong(v) == 0x7FF4DEADBEEF0001LL;
+}
+__device__ __forceinline__ bool is_sentinel(float v) { return __float_as_int(v) == 0x7FA0DEAD; }
+__device__ __forceinline__ double publishable(double v) {
+  return is_sentinel(v) ? __longlong_as_double(0x7FF8000000000000LL) : v;
+}
+__device__ __forceinline__ float publishable(float v) {
+  return is_sentinel(v) ? __int_as_float(0x7FC00000) : v;
+}
+template <typename T> __device__ __forceinline__ T sentinel();
+template <> __device__ __forceinline__ double sentinel<double>() { return sentinel_f64(); }
+template <> __device__ __forceinline__ float sentinel<float>() { return sentinel_f32(); }
+
+// --------------------------------------------------------------- memory ops
+__device__ __forceinline__ double ld_relaxed(const double* p) {
+  double v;
+  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ float ld_relaxed(const float* p) {
+  float v;
+  asm volatile("ld.relaxed.gpu.global.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed(double* p, double v) {
+  asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed(float* p, float v) {
+  asm volatile("st.relaxed.gpu.global.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_volatile(const int* p) {
+  return *reinterpret_cast<const volatile int*>(p);
+}
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wall-clock budget for any single spin-wait (ns).  Generous compared with
+// a whole solve (milliseconds) yet short enough that a broken dependency
+// returns an error in about a second instead of hanging the GPU.  The error
+// word array `err` (4 ints) carries the status in err[0] and an optional
+// override of the budget as a uint64 in err[2..3] (0 = this default).
+constexpr uint64_t kSpinBudgetNs = 1000000000ull;
+constexpr unsigned kPollCheck = 31u;  // check clock / abort every 32 polls
+
+__device__ __forceinline__ uint64_t spin_budget(const int* err) {
+  const uint64_t b = *reinterpret_cast<const volatile unsigned long long*>(err + 2);
+  return b ? b : kSpinBudgetNs;
+}
+
+// Spin until *p holds a computed value.  On timeout (or when another waiter
+// already timed out, signalled through *err) returns a quiet NaN and records
+// GB_TIMEOUT in *err.
+template <typename T>
+__device__ __forceinline__ T wait_value(const T* p, int* err) {
+  T v = ld_relaxed(p);
+  if (!is_sentinel(v)) return v;
+  const uint64_t t0 = globaltimer_ns();
+  const uint64_t budget = spin_budget(err);
+  unsigned polls = 0;
+  while (true) {
+    v = ld_relaxed(p);
+    if (!is_sentinel(v)) return v;
+    if ((++polls & kPollCheck) == 0u) {
+      if (ld_volatile(err) != 0 || globaltimer_ns() - t0 > budget) {
+        atomicCAS(err, 0, (int)GB_TIMEOUT);
+        return (T)__int_as_float(0x7FC00000);
+      }
+    }
+  }
+}
+
+// Spin until *flag != 0 (acquire).  Returns false on timeout / abort.
+__device__ __forceinline__ bool wait_flag(const int* flag, int* err) {
+  if (ld_acquire(flag) != 0) return true;
+  const uint64_t t0 = globaltimer_ns();
+  const uint64_t budget = spin_budget(err);
+  unsigned polls = 0;
+  while (true) {
+    if (ld_acquire(flag) != 0) return true;
+    if ((++polls & kPollCheck) == 0u) {
+      if (ld_volatile(err) != 0 || globaltimer_ns() - t0 > budget) {
+        atomicCAS(err, 0, (int)GB_TIMEOUT);
+        return false;
+      }
+    }
+  }
+}
+
+// --------------------------------------------------------------- reductions
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block sum of NV doubles; result valid in thread 0.  `sm` needs
+// NV * (blockDim/32) doubles.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* sm) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sm[k * nw + wid] = v[k];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double s = 0.0;
+      for (int w = 0; w < nw; ++w) s += sm[k * nw + w];
+      v[k] = s;
+    }
+  }
+}
+
+// Publishes this block's NV partials into part[k*stride + slot] and returns
+// true in thread 0 of exactly one block: the last to arrive.  That block then
+// sums the partials in slot order (deterministic) via final_sum().  The
+// ticket counter is reset by the last block, so the next launch reuses it.
+template <int NV>
+__device__ __forceinline__ bool publish_partials(const double (&v)[NV], double* part, int stride,
+                                                 int slot, unsigned* ticket, int nslots) {
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) part[k * stride + slot] = v[k];
+    __threadfence();
+    const unsigned t = atomicAdd(ticket, 1u);
+    last = (t == (unsigned)nslots - 1u);
+    if (last) {
+      *ticket = 0u;
+      __threadfence();
+    }
+  }
+  __syncthreads();
+  return last;
+}
+
+template <int NV>
+__device__ __forceinline__ void final_sum(double (&out)[NV], const double* part, int stride,
+                                          int nslots) {
+  // thread 0 only; volatile reads see every block's fenced write
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double s = 0.0;
+    const volatile double* pp = part + k * stride;
+    for (int i = 0; i < nslots; ++i) s += pp[i];
+    out[k] = s;
+  }
+}
+
+__host__ __device__ inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace gb

@@ -1,0 +1,40 @@
+// kernels.h -- host-side launchers of the generic kernels (kernels.cu).
+#pragma once
+
+#include "gblap_internal.h"
+
+namespace gb {
+
+int device_sm_count();
+
+// Greedy row bundles for `rows_per_bundle` <= 32 rows and <= kBundleNnz entries.
+int spmv_plan_build(int n, int nnz, const int* ia_host, SpmvPlan* plan, int rows_per_bundle);
+void spmv_plan_free(SpmvPlan* plan);
+
+// y = alpha*A*x + beta*y; plan may be null (plan-free 32-row bundles).
+template <typename T>
+int spmv_axpby(const SpmvPlan* plan, int n, const int* ia, const int* ja, const T* a, T alpha,
+               const T* x, T beta, T* y, cudaStream_t s);
+
+// Deterministic dot product; result written to *out_dev (device) and, if
+// out_host != null, copied back (synchronises the stream).
+int dot_dev(int n, const double* v, const double* w, double* out_dev, double* part,
+            unsigned* ticket, cudaStream_t s);
+
+int axpy_dev(int n, double alpha, const double* x, double* y, cudaStream_t s);
+int scal_dev(int n, double alpha, double* v, cudaStream_t s);
+int vec_vec_dev(int n, const double* x, const double* y, double* res, cudaStream_t s);
+int reciprocal_dev(int n, const double* v, double* res, cudaStream_t s);
+int sqrt_dev(int n, const double* v, double* res, cudaStream_t s);
+int copy_dev(int n, const double* src, double* dst, cudaStream_t s);
+int fill_dev(int n, double v, double* dst, cudaStream_t s);
+int fill_sentinel_dev(int n, double* dst, cudaStream_t s);
+int fill_sentinel_dev(int n, float* dst, cudaStream_t s);
+int cast_f64_to_f32(int n, const double* src, float* dst, cudaStream_t s);
+int cast_f32_to_f64(int n, const float* src, double* dst, cudaStream_t s);
+int gather_values(int n, const int* map, const double* src, double* dst, float* dst32,
+                  cudaStream_t s);
+
+int reduction_grid();
+
+}  // namespace gb

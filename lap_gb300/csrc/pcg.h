@@ -1,0 +1,42 @@
+// pcg.h -- launchers of the fused PCG kernels (pcg.cu) and the composed
+// preconditioners (precond.cu).
+#pragma once
+
+#include "gblap_internal.h"
+#include "system.h"
+
+namespace gb {
+
+int prec_wkind(int prec, int k);
+bool prec_fused_tri(int prec, int k);
+int part_len_needed(gb_system sys);
+
+template <typename T>
+int launch_prologue(gb_system sys, PcgState* st, int x_zero, const T* b);
+template <typename T>
+int launch_body(gb_system sys, PcgState* st, cudaGraphConditionalHandle cond, int has_cond);
+
+int launch_true_resid(gb_system sys, const double* b, const double* x, double* out2);
+int launch_outer_resid(gb_system sys, const double* b, const double* x, int first);
+int launch_add_correction(gb_system sys, double* x);
+
+// LAP's preconditioners that are compositions of SpMV / BLAS-1 calls
+// (it_jacobi.c, GS.c GS_it / GS_it2, GS_std with k > 1, and line_jacobi /
+// none for completeness): y = M^{-1} x, FP64, on the system stream.
+int apply_prec_composed(gb_system sys, const double* x, double* y);
+// Any preconditioner (including the sync-free GS_std / ichol solves).
+int apply_prec(gb_system sys, const double* x, double* y);
+
+// Per-kernel timing hook used by gb_profile_iteration: while set, every PCG
+// kernel launch is followed by an event record on the system stream.
+struct ProfHook {
+  static constexpr int kMax = 32;
+  int count = 0;
+  cudaEvent_t ev[kMax];
+  const char* name[kMax];
+  double bytes[kMax];
+};
+extern ProfHook* g_prof;
+void prof_mark(cudaStream_t s, const char* name, double bytes);
+
+}  // namespace gb

@@ -1,0 +1,50 @@
+// sptrsv.h -- level schedules for the sync-free triangular solves and IC(0).
+#pragma once
+
+#include <vector>
+
+#include "gblap_internal.h"
+
+namespace gb {
+
+// Dependency description of one triangular factor, in summation order:
+// row i depends on dep_col[row_ptr[i] .. row_ptr[i+1]) whose values live at
+// ent_src[dep_src[..]]; its diagonal at diag_src_arr[diag_src[i]].
+struct TriDeps {
+  int n = 0;
+  bool lower = true;
+  std::vector<int> row_ptr, dep_col, dep_src, diag_src;
+};
+
+// LAP GPU convention: diagonal stored inside the factor (last in an L row,
+// first in a U row, but found anywhere in the row).  Returns GB_BAD_INPUT
+// when a row has no diagonal or a dependency on the wrong side.
+int deps_embedded(int n, const int* ia, const int* ja, bool lower, TriDeps* d);
+// LAP CPU convention: strict factor, diagonal in a separate array (index i).
+int deps_strict(int n, const int* ia, const int* ja, bool lower, TriDeps* d);
+// IC(0) on A's full pattern: lower = A's strict-lower entries, upper = L^T
+// read through the transpose positions; values come from the factor stored
+// on A's pattern.  tpos[k] = index of entry (j, i) for entry k = (i, j).
+int transpose_positions(int n, const int* ia, const int* ja, std::vector<int>* tpos);
+int deps_ichol(int n, const int* ia, const int* ja, const std::vector<int>& tpos, bool lower,
+               TriDeps* d);
+
+int tri_plan_build(const TriDeps& d, TriPlan* plan);
+void tri_plan_free(TriPlan* plan);
+// eval/diag (and their FP32 copies when want32) from value arrays.
+int tri_plan_fill(TriPlan* plan, const double* ent_src, const double* diag_src, bool want32,
+                  cudaStream_t s);
+
+// y = T^{-1} x with the plan's values.  y must not alias x.
+template <typename T>
+int tri_solve_plain(const TriPlan* plan, const T* x, T* y, int* err, cudaStream_t s);
+
+// IC(0) factorization on A's pattern (left-looking, sync-free, level order
+// of the lower schedule).  f receives the factor in symmetric storage: the
+// strict-lower entries hold L, the diagonal sqrt pivots, the strict upper
+// L^T.  zero_pivot (device int) receives the first offending row + 1 or 0.
+int ichol_factor_dev(int n, const int* ia, const int* ja, const double* a, const int* dpos,
+                     const int* tpos, const TriPlan* lower_plan, double* f, int* done,
+                     unsigned* ticket, int* zero_pivot, int* err, cudaStream_t s);
+
+}  // namespace gb

@@ -1,0 +1,577 @@
+// system.cu -- gb_system: setup (validation, SpMV plan, level schedules,
+// on-device IC(0)), the solve drivers (CUDA-graph while loop or eager), the
+// FP32-inner / FP64-refinement solve, and the kernel-level entry points.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "gb_common.cuh"
+#include "kernels.h"
+#include "pcg.h"
+#include "pcg_state.cuh"
+#include "sptrsv.h"
+#include "system.h"
+
+using namespace gb;
+
+// ------------------------------------------------------------ names / status
+extern "C" const char* gb_status_str(int s) {
+  switch (s) {
+    case GB_OK: return "ok";
+    case GB_MAXIT: return "maximum iterations reached";
+    case GB_BREAKDOWN: return "breakdown (p'q <= 0 or non-finite)";
+    case GB_ZERO_PIVOT: return "IC(0) zero or negative pivot";
+    case GB_TIMEOUT: return "sync-free wait timed out";
+    case GB_BAD_INPUT: return "bad input";
+    case GB_CUDA_ERROR: return "CUDA error";
+    case GB_NO_MEMORY: return "out of device memory";
+    case GB_NOT_SUPPORTED: return "not supported";
+  }
+  return "unknown status";
+}
+
+extern "C" int gb_prec_from_name(const char* name) {
+  if (!name) return -1;
+  static const char* names[] = {"none", "line_jacobi", "it_jacobi", "GS_std", "GS_it", "GS_it2", "ichol"};
+  for (int i = 0; i < 7; ++i)
+    if (strcmp(name, names[i]) == 0) return i;
+  return -1;
+}
+
+extern "C" const char* gb_version(void) { return "libgblap 0.1 (sm_103a, CUDA " GB_STR(__CUDACC_VER_MAJOR__) ")"; }
+
+extern "C" void gb_pcg_opts_default(gb_pcg_opts* o) {
+  if (!o) return;
+  o->tol = 1e-8;
+  o->maxit = 10000;
+  o->precision = 0;
+  o->inner_tol = 1e-4;
+  o->max_outer = 50;
+  o->use_graph = 1;
+  o->verbose = 0;
+}
+
+// ------------------------------------------------------------ helpers
+namespace {
+
+template <typename V>
+int dalloc(V** p, size_t count) {
+  cudaError_t e = cudaMalloc((void**)p, sizeof(V) * std::max<size_t>(count, 1));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return e == cudaErrorMemoryAllocation ? GB_NO_MEMORY : GB_CUDA_ERROR;
+  }
+  return GB_OK;
+}
+template <typename V>
+int dupload(V** p, const std::vector<V>& h) {
+  GB_TRY(dalloc(p, h.size()));
+  if (!h.empty()) GB_CUDA_TRY(cudaMemcpy(*p, h.data(), sizeof(V) * h.size(), cudaMemcpyHostToDevice));
+  return GB_OK;
+}
+
+// Full symmetric CSR -> strict one-sided dependency list, diagonal from A.
+int deps_from_full(int n, const int* ia, const int* ja, const std::vector<int>& dpos, bool lower,
+                   TriDeps* d) {
+  d->n = n;
+  d->lower = lower;
+  d->row_ptr.assign(n + 1, 0);
+  d->diag_src = dpos;
+  d->dep_col.clear();
+  d->dep_src.clear();
+  for (int i = 0; i < n; ++i) {
+    for (int k = ia[i]; k < ia[i + 1]; ++k) {
+      const int c = ja[k];
+      if ((lower && c < i) || (!lower && c > i)) {
+        d->dep_col.push_back(c);
+        d->dep_src.push_back(k);
+      }
+    }
+    d->row_ptr[i + 1] = (int)d->dep_col.size();
+  }
+  return GB_OK;
+}
+
+void init_state_host(PcgState* h, double tol, int maxit, int hist_len) {
+  memset(h, 0, sizeof(*h));
+  h->spare0 = tol;
+  h->maxit = maxit;
+  h->hist_len = hist_len;
+  h->flag = 1;
+  h->status = GB_OK;
+}
+
+}  // namespace
+
+namespace gb {
+int system_ensure_hist(gb_system sys, int maxit) {
+  const int need = maxit + 3;
+  if (sys->hist_cap >= need) return GB_OK;
+  if (sys->hist) cudaFree(sys->hist);
+  sys->hist = nullptr;
+  GB_TRY(dalloc(&sys->hist, need));
+  sys->hist_cap = need;
+  for (auto& lg : sys->loop) {  // graphs captured the old pointer
+    if (lg.exec) cudaGraphExecDestroy(lg.exec);
+    if (lg.graph) cudaGraphDestroy(lg.graph);
+    lg = LoopGraph();
+  }
+  sys->loop_key[0] = sys->loop_key[1] = -1;
+  return GB_OK;
+}
+}  // namespace gb
+
+static void system_free(gb_system s) {
+  if (!s) return;
+  for (auto& lg : s->loop) {
+    if (lg.exec) cudaGraphExecDestroy(lg.exec);
+    if (lg.graph) cudaGraphDestroy(lg.graph);
+  }
+  spmv_plan_free(&s->plan);
+  tri_plan_free(&s->L);
+  tri_plan_free(&s->U);
+  void* ptrs[] = {s->dpos, s->tpos, s->diag, s->d_r, s->d_r32, s->a32, s->fac, s->fac_done,
+                  s->zero_pivot, s->fac_ticket, s->lia, s->lja, s->uia, s->uja, s->la, s->ua,
+                  s->v64.x, s->v64.r, s->v64.w, s->v64.p0, s->v64.p1, s->v64.q, s->v64.t,
+                  s->v64.s, s->v32.x, s->v32.r, s->v32.w, s->v32.p0, s->v32.p1, s->v32.q,
+                  s->v32.t, s->v32.s, s->b_int, s->aux1, s->aux2, s->aux3, s->part, s->st,
+                  s->st_out, s->hist, s->err, s->lower_idx, s->lower_row, s->lmap_cpu,
+                  s->umap_cpu, s->scratch, s->edge_idx, s->edge_row};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (s->st_host) cudaFreeHost(s->st_host);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->s) cudaStreamDestroy(s->s);
+  delete s;
+}
+
+// Validates a full symmetric CSR (0-based, sorted, no duplicates, diagonal
+// stored).  LAP itself does not check (io_utils.c:141-363 trusts its input;
+// a missing diagonal corrupts memory in split()).
+static int validate_csr(int n, int nnz, const std::vector<int>& ia, const std::vector<int>& ja,
+                        std::vector<int>* dpos) {
+  if (ia[0] != 0 || ia[n] != nnz) return GB_BAD_INPUT;
+  dpos->assign(n, -1);
+  for (int i = 0; i < n; ++i) {
+    if (ia[i + 1] < ia[i]) return GB_BAD_INPUT;
+    int prev = -1;
+    for (int k = ia[i]; k < ia[i + 1]; ++k) {
+      const int c = ja[k];
+      if (c < 0 || c >= n || c <= prev) return GB_BAD_INPUT;
+      prev = c;
+      if (c == i) (*dpos)[i] = k;
+    }
+    if ((*dpos)[i] < 0) return GB_BAD_INPUT;
+  }
+  return GB_OK;
+}
+
+static int setup_values(gb_system s) {
+  const int n = s->n;
+  GB_TRY(gather_values(n, s->dpos, s->a, s->diag, nullptr, s->s));
+  GB_TRY(reciprocal_dev(n, s->diag, s->d_r, s->s));
+  GB_TRY(cast_f64_to_f32(n, s->d_r, s->d_r32, s->s));
+  GB_TRY(cast_f64_to_f32(s->nnz, s->a, s->a32, s->s));
+  if (s->prec == GB_PREC_GS_STD) {
+    GB_TRY(tri_plan_fill(&s->L, s->a, s->a, true, s->s));
+    GB_TRY(tri_plan_fill(&s->U, s->a, s->a, true, s->s));
+  } else if (s->prec == GB_PREC_ICHOL) {
+    GB_TRY(ichol_factor_dev(n, s->ia, s->ja, s->a, s->dpos, s->tpos, &s->L, s->fac, s->fac_done,
+                            s->fac_ticket, s->zero_pivot, s->err, s->s));
+    GB_TRY(tri_plan_fill(&s->L, s->fac, s->fac, true, s->s));
+    GB_TRY(tri_plan_fill(&s->U, s->fac, s->fac, true, s->s));
+  } else if (s->prec == GB_PREC_IT_JACOBI || s->prec == GB_PREC_GS_IT || s->prec == GB_PREC_GS_IT2) {
+    GB_TRY(gather_values(s->lnnz, s->lmap_cpu, s->a, s->la, nullptr, s->s));
+    GB_TRY(gather_values(s->unnz, s->umap_cpu, s->a, s->ua, nullptr, s->s));
+  }
+  GB_CUDA_TRY(cudaStreamSynchronize(s->s));
+  if (s->prec == GB_PREC_ICHOL) {
+    int zp = 0, err = 0;
+    GB_CUDA_TRY(cudaMemcpy(&zp, s->zero_pivot, sizeof(int), cudaMemcpyDeviceToHost));
+    GB_CUDA_TRY(cudaMemcpy(&err, s->err, sizeof(int), cudaMemcpyDeviceToHost));
+    s->zero_pivot_row = zp;
+    if (err) return err;
+  }
+  return GB_OK;
+}
+
+extern "C" int gb_system_create(int n, int nnz, const int* ia, const int* ja, const double* a,
+                                const char* prec_name, int m, int k, gb_system* out) {
+  if (!out) return GB_BAD_INPUT;
+  *out = nullptr;
+  const int prec = gb_prec_from_name(prec_name);
+  if (n <= 0 || nnz < n || !ia || !ja || !a || prec < 0 || m < 0 || k < 0) return GB_BAD_INPUT;
+  gb_system s = new gb_system_s();
+  s->n = n;
+  s->nnz = nnz;
+  s->ia = ia;
+  s->ja = ja;
+  s->a = a;
+  s->prec = prec;
+  s->m = m;
+  s->k = k;
+  int rc = GB_OK;
+#define CK(expr)            \
+  do {                      \
+    rc = (expr);            \
+    if (rc != GB_OK) {      \
+      system_free(s);       \
+      return rc;            \
+    }                       \
+  } while (0)
+#define CKC(expr) CK((expr) == cudaSuccess ? GB_OK : GB_CUDA_ERROR)
+  CKC(cudaStreamCreateWithFlags(&s->s, cudaStreamNonBlocking));
+  CKC(cudaEventCreate(&s->ev0));
+  CKC(cudaEventCreate(&s->ev1));
+  s->h_ia.resize(n + 1);
+  s->h_ja.resize(nnz);
+  CKC(cudaMemcpy(s->h_ia.data(), ia, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
+  CKC(cudaMemcpy(s->h_ja.data(), ja, sizeof(int) * (size_t)nnz, cudaMemcpyDeviceToHost));
+  std::vector<int> dpos;
+  CK(validate_csr(n, nnz, s->h_ia, s->h_ja, &dpos));
+  CK(spmv_plan_build(n, nnz, s->h_ia.data(), &s->plan, kBundleRows));
+  CK(dupload(&s->dpos, dpos));
+  CK(dalloc(&s->diag, n));
+  CK(dalloc(&s->d_r, n));
+  CK(dalloc(&s->d_r32, n));
+  CK(dalloc(&s->a32, nnz));
+  CK(dalloc(&s->err, 4));
+  CKC(cudaMemset(s->err, 0, sizeof(int) * 4));
+  const int* hia = s->h_ia.data();
+  const int* hja = s->h_ja.data();
+  std::vector<int> tpos;
+  CK(transpose_positions(n, hia, hja, &tpos));  // also proves the pattern symmetric
+  CK(dupload(&s->tpos, tpos));
+  if (prec == GB_PREC_GS_STD || prec == GB_PREC_ICHOL) {
+    s->tri = true;
+    TriDeps dl, du;
+    if (prec == GB_PREC_GS_STD) {
+      CK(deps_from_full(n, hia, hja, dpos, true, &dl));
+      CK(deps_from_full(n, hia, hja, dpos, false, &du));
+    } else {
+      CK(deps_ichol(n, hia, hja, tpos, true, &dl));
+      CK(deps_ichol(n, hia, hja, tpos, false, &du));
+      CK(dalloc(&s->fac, nnz));
+      CK(dalloc(&s->fac_done, n));
+      CK(dalloc(&s->zero_pivot, 1));
+      CK(dalloc(&s->fac_ticket, 4));
+      CKC(cudaMemset(s->fac_ticket, 0, sizeof(unsigned) * 4));
+    }
+    CK(tri_plan_build(dl, &s->L));
+    CK(tri_plan_build(du, &s->U));
+  }
+  if (prec == GB_PREC_IT_JACOBI || prec == GB_PREC_GS_IT || prec == GB_PREC_GS_IT2) {
+    std::vector<int> lp(n + 1, 0), up(n + 1, 0), lj, uj, lm, um;
+    for (int i = 0; i < n; ++i) {
+      for (int q = hia[i]; q < hia[i + 1]; ++q) {
+        if (hja[q] < i) { lj.push_back(hja[q]); lm.push_back(q); }
+        if (hja[q] > i) { uj.push_back(hja[q]); um.push_back(q); }
+      }
+      lp[i + 1] = (int)lj.size();
+      up[i + 1] = (int)uj.size();
+    }
+    s->lnnz = (int)lj.size();
+    s->unnz = (int)uj.size();
+    CK(dupload(&s->lia, lp));
+    CK(dupload(&s->uia, up));
+    CK(dupload(&s->lja, lj));
+    CK(dupload(&s->uja, uj));
+    CK(dupload(&s->lmap_cpu, lm));
+    CK(dupload(&s->umap_cpu, um));
+    CK(dalloc(&s->la, s->lnnz));
+    CK(dalloc(&s->ua, s->unnz));
+  }
+  // work vectors
+  for (double** p : {&s->v64.x, &s->v64.r, &s->v64.w, &s->v64.p0, &s->v64.p1, &s->v64.q,
+                     &s->v64.t, &s->v64.s, &s->b_int, &s->aux1, &s->aux2, &s->aux3})
+    CK(dalloc(p, n));
+  for (float** p : {&s->v32.x, &s->v32.r, &s->v32.w, &s->v32.p0, &s->v32.p1, &s->v32.q,
+                    &s->v32.t, &s->v32.s})
+    CK(dalloc(p, n));
+  s->part_len = part_len_needed(s);
+  CK(dalloc(&s->part, s->part_len));
+  CK(dalloc(&s->st, 1));
+  CK(dalloc(&s->st_out, 1));
+  CK(dalloc(&s->scratch, 8));
+  CKC(cudaMemset(s->st, 0, sizeof(PcgState)));
+  CKC(cudaMemset(s->st_out, 0, sizeof(PcgState)));
+  CKC(cudaMallocHost(&s->st_host, sizeof(PcgState) * 2));
+  CK(system_ensure_hist(s, 1000));
+  CK(setup_values(s));
+#undef CK
+#undef CKC
+  *out = s;
+  return GB_OK;
+}
+
+extern "C" int gb_system_destroy(gb_system s) {
+  if (!s) return GB_BAD_INPUT;
+  cudaStreamSynchronize(s->s);
+  system_free(s);
+  return GB_OK;
+}
+
+extern "C" int gb_debug_set_spin_budget(gb_system s, unsigned long long ns) {
+  if (!s) return GB_BAD_INPUT;
+  GB_CUDA_TRY(cudaMemcpy(s->err + 2, &ns, sizeof ns, cudaMemcpyHostToDevice));
+  return GB_OK;
+}
+
+extern "C" int gb_system_update_values(gb_system s) {
+  if (!s) return GB_BAD_INPUT;
+  return setup_values(s);
+}
+
+extern "C" int gb_system_info(gb_system s, int* lower_levels, int* upper_levels, int* tiles) {
+  if (!s) return GB_BAD_INPUT;
+  if (lower_levels) *lower_levels = s->L.nlevels;
+  if (upper_levels) *upper_levels = s->U.nlevels;
+  if (tiles) *tiles = s->plan.nbundles;
+  return s->zero_pivot_row ? GB_ZERO_PIVOT : GB_OK;
+}
+
+// ------------------------------------------------------------ solve loop
+// Builds (once) a graph holding only a while node whose body is one PCG
+// iteration; the body's checking kernel sets the condition.
+template <typename T>
+static int get_loop_graph(gb_system s, int idx, LoopGraph** out) {
+  LoopGraph* lg = &s->loop[idx];
+  const int key = s->hist_cap;
+  if (lg->exec && s->loop_key[idx] == key) {
+    *out = lg;
+    return GB_OK;
+  }
+  if (lg->exec) cudaGraphExecDestroy(lg->exec);
+  if (lg->graph) cudaGraphDestroy(lg->graph);
+  *lg = LoopGraph();
+  cudaGraph_t g;
+  GB_CUDA_TRY(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle h;
+  GB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+  // cudaGraphNodeParams has no usable default constructor in C++; start from
+  // zeroed storage as the C API expects
+  alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)];
+  memset(cp_buf, 0, sizeof cp_buf);
+  cudaGraphNodeParams& cp = *reinterpret_cast<cudaGraphNodeParams*>(cp_buf);
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  GB_CUDA_TRY(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  GB_CUDA_TRY(cudaStreamBeginCaptureToGraph(s->s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  const int rc = launch_body<T>(s, s->st, h, 1);
+  cudaGraph_t captured = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(s->s, &captured);
+  if (rc != GB_OK || e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    return rc != GB_OK ? rc : GB_CUDA_ERROR;
+  }
+  GB_CUDA_TRY(cudaGraphInstantiate(&lg->exec, g, 0));
+  lg->graph = g;
+  s->loop_key[idx] = key;
+  *out = lg;
+  return GB_OK;
+}
+
+// Runs one PCG recurrence on the system stream: prologue, then the loop.
+template <typename T>
+static int run_recurrence(gb_system s, double tol, int maxit, int x_zero, const T* b, int use_graph) {
+  const int idx = sizeof(T) == 8 ? 0 : 1;
+  init_state_host(s->st_host, tol, maxit, s->hist_cap);
+  GB_CUDA_TRY(cudaMemcpyAsync(s->st, s->st_host, sizeof(PcgState), cudaMemcpyHostToDevice, s->s));
+  GB_TRY(launch_prologue<T>(s, s->st, x_zero, b));
+  if (use_graph) {
+    LoopGraph* lg = nullptr;
+    GB_TRY(get_loop_graph<T>(s, idx, &lg));
+    GB_CUDA_TRY(cudaGraphLaunch(lg->exec, s->s));
+  } else {
+    // eager: a status read every 16 iterations
+    for (int it = 0; it <= maxit + 1; it += 16) {
+      for (int j = 0; j < 16; ++j) GB_TRY(launch_body<T>(s, s->st, 0, 0));
+      GB_CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(PcgState), cudaMemcpyDeviceToHost, s->s));
+      GB_CUDA_TRY(cudaStreamSynchronize(s->s));
+      if (s->st_host->done) break;
+    }
+  }
+  return GB_OK;
+}
+
+static int read_state(gb_system s, PcgState* dst, const PcgState* src) {
+  GB_CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(PcgState), cudaMemcpyDeviceToHost, s->s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s->s));
+  return GB_OK;
+}
+
+// Core solve on the internal buffers b_int (rhs) and v64.x (x0 -> x).
+static int solve_internal(gb_system s, const gb_pcg_opts* o, gb_pcg_result* res, double* hist_host,
+                          int hist_len) {
+  GB_TRY(system_ensure_hist(s, o->maxit));
+  GB_CUDA_TRY(cudaMemsetAsync(s->err, 0, sizeof(int), s->s));
+  gb_pcg_result r;
+  memset(&r, 0, sizeof r);
+  PcgState* hs = s->st_host;
+  if (o->precision == 0) {
+    GB_TRY(run_recurrence<double>(s, o->tol, o->maxit, 0, s->b_int, o->use_graph));
+    GB_TRY(launch_true_resid(s, s->b_int, s->v64.x, s->scratch));
+    GB_TRY(read_state(s, hs, s->st));
+    r.iters = hs->iter;
+    r.flag = hs->flag;
+    r.status = hs->status;
+    r.res0 = hs->res0;
+    r.res = std::sqrt(hs->rr);
+    if (hist_host && hist_len > 0) {
+      const int cnt = std::min(hist_len, std::min(hs->iter + 1, s->hist_cap));
+      GB_CUDA_TRY(cudaMemcpy(hist_host, s->hist, sizeof(double) * cnt, cudaMemcpyDeviceToHost));
+    }
+  } else {
+    if (!(s->prec == GB_PREC_LINE_JACOBI || s->prec == GB_PREC_NONE || prec_fused_tri(s->prec, s->k)))
+      return GB_NOT_SUPPORTED;
+    PcgState* ho = s->st_host + 1;
+    init_state_host(ho, o->tol, o->maxit, 0);
+    GB_CUDA_TRY(cudaMemcpyAsync(s->st_out, ho, sizeof(PcgState), cudaMemcpyHostToDevice, s->s));
+    int total = 0, outer = 0, flag = 1, status = GB_MAXIT;
+    double last_res = 0.0;
+    for (;;) {
+      GB_TRY(launch_outer_resid(s, s->b_int, s->v64.x, outer == 0));
+      GB_TRY(read_state(s, ho, s->st_out));
+      last_res = std::sqrt(ho->rr);
+      if (hist_host && outer < hist_len) hist_host[outer] = last_res;
+      if (ho->done) {
+        flag = ho->flag;
+        status = ho->status;
+        break;
+      }
+      if (outer >= o->max_outer || total > o->maxit) break;
+      const int budget = std::max(1, o->maxit - total);
+      GB_TRY(run_recurrence<float>(s, o->inner_tol, budget, 1, s->v32.r, o->use_graph));
+      GB_TRY(read_state(s, hs, s->st));
+      total += hs->iter;
+      if (hs->status == GB_BREAKDOWN && hs->iter <= 1) {
+        flag = 2;
+        status = GB_BREAKDOWN;
+        break;
+      }
+      GB_TRY(launch_add_correction(s, s->v64.x));
+      ++outer;
+    }
+    r.iters = total;
+    r.outer = outer;
+    r.flag = flag;
+    r.status = status;
+    r.res0 = ho->res0;
+    r.res = last_res;
+    GB_TRY(launch_true_resid(s, s->b_int, s->v64.x, s->scratch));
+  }
+  double tr[2] = {0.0, 0.0};
+  GB_CUDA_TRY(cudaMemcpyAsync(tr, s->scratch, sizeof tr, cudaMemcpyDeviceToHost, s->s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s->s));
+  int err = 0;
+  GB_CUDA_TRY(cudaMemcpy(&err, s->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) r.status = err;
+  r.true_res = tr[0];
+  r.rel_true_res = tr[1] > 0.0 ? tr[0] / tr[1] : tr[0];
+  if (o->verbose && hist_host)
+    for (int i = 0; i <= std::min(r.iters, hist_len - 1); ++i)
+      printf("CG: it %d, res norm %5.5e \n", i, hist_host[i]);
+  if (res) *res = r;
+  return r.status == GB_TIMEOUT ? GB_TIMEOUT : GB_OK;
+}
+
+extern "C" int gb_pcg_solve(gb_system s, const double* b, double* x, const gb_pcg_opts* opts,
+                            double* hist_host, int hist_len, gb_pcg_result* res) {
+  if (!s || !b || !x) return GB_BAD_INPUT;
+  gb_pcg_opts o;
+  if (opts) o = *opts;
+  else gb_pcg_opts_default(&o);
+  if (o.maxit < 0 || !(o.tol >= 0.0)) return GB_BAD_INPUT;
+  const size_t bytes = sizeof(double) * s->n;
+  GB_CUDA_TRY(cudaEventRecord(s->ev0, s->s));
+  GB_CUDA_TRY(cudaMemcpyAsync(s->b_int, b, bytes, cudaMemcpyDeviceToDevice, s->s));
+  GB_CUDA_TRY(cudaMemcpyAsync(s->v64.x, x, bytes, cudaMemcpyDeviceToDevice, s->s));
+  const int rc = solve_internal(s, &o, res, hist_host, hist_len);
+  GB_CUDA_TRY(cudaMemcpyAsync(x, s->v64.x, bytes, cudaMemcpyDeviceToDevice, s->s));
+  GB_CUDA_TRY(cudaEventRecord(s->ev1, s->s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s->s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+  if (res) res->device_ms = ms;
+  return rc;
+}
+
+extern "C" int gb_pcg_solve_host(gb_system s, const double* b_host, double* x_host,
+                                 const gb_pcg_opts* opts, gb_pcg_result* res) {
+  if (!s || !b_host || !x_host) return GB_BAD_INPUT;
+  gb_pcg_opts o;
+  if (opts) o = *opts;
+  else gb_pcg_opts_default(&o);
+  const size_t bytes = sizeof(double) * s->n;
+  GB_CUDA_TRY(cudaEventRecord(s->ev0, s->s));
+  GB_CUDA_TRY(cudaMemcpyAsync(s->b_int, b_host, bytes, cudaMemcpyHostToDevice, s->s));
+  GB_CUDA_TRY(cudaMemcpyAsync(s->v64.x, x_host, bytes, cudaMemcpyHostToDevice, s->s));
+  const int rc = solve_internal(s, &o, res, nullptr, 0);
+  GB_CUDA_TRY(cudaMemcpyAsync(x_host, s->v64.x, bytes, cudaMemcpyDeviceToHost, s->s));
+  GB_CUDA_TRY(cudaEventRecord(s->ev1, s->s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s->s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+  if (res) res->device_ms = ms;
+  return rc;
+}
+
+// ------------------------------------------------------------ kernels
+extern "C" int gb_spmv(gb_system s, double alpha, const double* x, double beta, double* y) {
+  if (!s || !x || !y) return GB_BAD_INPUT;
+  GB_TRY(spmv_axpby<double>(&s->plan, s->n, s->ia, s->ja, s->a, alpha, x, beta, y, s->s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s->s));
+  return GB_OK;
+}
+
+extern "C" int gb_precond_apply(gb_system s, const double* x, double* y) {
+  if (!s || !x || !y || x == y) return GB_BAD_INPUT;
+  GB_CUDA_TRY(cudaMemsetAsync(s->err, 0, sizeof(int), s->s));
+  GB_TRY(apply_prec(s, x, y));
+  GB_CUDA_TRY(cudaStreamSynchronize(s->s));
+  int err = 0;
+  GB_CUDA_TRY(cudaMemcpy(&err, s->err, sizeof(int), cudaMemcpyDeviceToHost));
+  return err ? err : GB_OK;
+}
+
+extern "C" int gb_ichol_factor_values(gb_system s, double* l_vals, double* u_vals) {
+  if (!s || s->prec != GB_PREC_ICHOL) return GB_BAD_INPUT;
+  // LAP CPU layout: L rows = strict lower entries then the diagonal; U rows =
+  // diagonal then strict upper entries (cg_driver2.c:146-196).
+  if (!s->lower_idx) {
+    const int n = s->n;
+    const int* hia = s->h_ia.data();
+    const int* hja = s->h_ja.data();
+    std::vector<int> lm, um;
+    for (int i = 0; i < n; ++i) {
+      int d = -1;
+      for (int q = hia[i]; q < hia[i + 1]; ++q) {
+        if (hja[q] < i) lm.push_back(q);
+        if (hja[q] == i) d = q;
+      }
+      lm.push_back(d);
+      um.push_back(d);
+      for (int q = hia[i]; q < hia[i + 1]; ++q)
+        if (hja[q] > i) um.push_back(q);
+    }
+    s->lu_len = (int)lm.size();
+    GB_TRY(dupload(&s->lower_idx, lm));
+    GB_TRY(dupload(&s->lower_row, um));
+  }
+  if (l_vals) GB_TRY(gather_values(s->lu_len, s->lower_idx, s->fac, l_vals, nullptr, s->s));
+  if (u_vals) GB_TRY(gather_values(s->lu_len, s->lower_row, s->fac, u_vals, nullptr, s->s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s->s));
+  return s->zero_pivot_row ? GB_ZERO_PIVOT : GB_OK;
+}

@@ -46,6 +46,8 @@ def _bind(lib: C.CDLL) -> C.CDLL:
                                   _dp, C.POINTER(C.c_double), C.c_int,
                                   C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.orc_num_threads.restype = C.c_int
+    lib.orc_prec_apply_csr.argtypes = [C.c_int, C.c_int, _ip, _ip, _dp, C.c_char_p, C.c_int,
+                                       C.c_int, _dp, _dp]
     return lib
 
 
@@ -163,6 +165,16 @@ def solve(n, ia, ja, a, b, prec="line_jacobi", tol=1e-8, maxit=10000, M=1, K=1,
                                  C.byref(tr), max_iters_run, C.byref(su), C.byref(so))
     return dict(x=x, iters=it, flag=flag.value, res_hist=hist[: it + 1].copy(),
                 true_res=tr.value, setup_s=su.value, solve_s=so.value)
+
+
+def prec_apply(n, ia, ja, a, x, prec, M=1, K=1):
+    """y = M^{-1} x: one prec_function call after the NOACC driver's setup."""
+    y = np.zeros(n)
+    lib().orc_prec_apply_csr(n, len(ja), np.ascontiguousarray(ia, dtype=np.int32),
+                             np.ascontiguousarray(ja, dtype=np.int32),
+                             np.ascontiguousarray(a, dtype=np.float64), prec.encode(), M, K,
+                             np.ascontiguousarray(x, dtype=np.float64), y)
+    return y
 
 
 def ref_solve(n, ia, ja, a, b, prec="line_jacobi", tol=1e-8, maxit=10000, M=1, K=1):

@@ -551,10 +551,34 @@ void orc_free(void *p) { free(p); }
 
 /* ---------------- one-call solve (cg_driver2.c NOACC path) ---------------- */
 
+/* One preconditioner application y = M^{-1} x after cg_driver2.c's NOACC
+ * setup (mode 0 = full run through orc_cg, used by orc_solve_csr; mode 1 =
+ * apply only). */
+static int run_csr(int n, int nnz, const int *ia, const int *ja, const double *a,
+                   const double *b, double *x, const char *prec, double tol, int maxit,
+                   int M, int K, int *flag, double *res_hist, double *true_res,
+                   int max_iters_run, double *setup_s, double *solve_s, int apply_only,
+                   const double *px, double *py);
+
+int orc_prec_apply_csr(int n, int nnz, const int *ia, const int *ja, const double *a,
+                       const char *prec, int M, int K, const double *x, double *y) {
+  return run_csr(n, nnz, ia, ja, a, NULL, NULL, prec, 0.0, 0, M, K, NULL, NULL, NULL, 0, NULL,
+                 NULL, 1, x, y);
+}
+
 int orc_solve_csr(int n, int nnz, const int *ia, const int *ja, const double *a,
                   const double *b, double *x, const char *prec, double tol, int maxit,
                   int M, int K, int *flag, double *res_hist, double *true_res,
                   int max_iters_run, double *setup_s, double *solve_s) {
+  return run_csr(n, nnz, ia, ja, a, b, x, prec, tol, maxit, M, K, flag, res_hist, true_res,
+                 max_iters_run, setup_s, solve_s, 0, NULL, NULL);
+}
+
+static int run_csr(int n, int nnz, const int *ia, const int *ja, const double *a,
+                  const double *b, double *x, const char *prec, double tol, int maxit,
+                  int M, int K, int *flag, double *res_hist, double *true_res,
+                   int max_iters_run, double *setup_s, double *solve_s, int apply_only,
+                   const double *px, double *py) {
   const double t0 = wall_s();
   orc_mmatrix A, L, U;
   memset(&A, 0, sizeof A);
@@ -578,8 +602,9 @@ int orc_solve_csr(int n, int nnz, const int *ia, const int *ja, const double *a,
   p.aux_vec2 = (double *)calloc((size_t)n + 1, sizeof(double));
   p.aux_vec3 = (double *)calloc((size_t)n + 1, sizeof(double));
   const double t1 = wall_s();
-  const int it = orc_cg(n, nnz, ia, ja, a, x, b, tol, &p, maxit, flag, res_hist, true_res,
-                        max_iters_run);
+  const int it = apply_only ? (orc_prec_function(ia, ja, a, nnz, &p, px, py), 0)
+                            : orc_cg(n, nnz, ia, ja, a, x, b, tol, &p, maxit, flag, res_hist,
+                                     true_res, max_iters_run);
   const double t2 = wall_s();
   if (setup_s) *setup_s = t1 - t0;
   if (solve_s) *solve_s = t2 - t1;

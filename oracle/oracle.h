@@ -119,6 +119,10 @@ int    orc_solve_csr(int n, int nnz, const int *ia, const int *ja, const double 
                      double *true_res, int max_iters_run,
                      double *setup_s, double *solve_s);
 
+/* y = M^{-1} x after the same setup (one prec_function call). */
+int    orc_prec_apply_csr(int n, int nnz, const int *ia, const int *ja, const double *a,
+                          const char *prec, int M, int K, const double *x, double *y);
+
 /* Number of OpenMP threads the multicore mirror uses (1 without OpenMP). */
 int    orc_num_threads(void);
 

@@ -1,0 +1,244 @@
+"""GPU parity of the device-resident PCG (gb_pcg_solve and LAP's cg()) against
+the reference's own results (golden fixtures) and the CPU oracle.
+
+Acceptance: relative residual <= tol, solution within 1e-6 relative of the
+reference's, iteration count within +-2% for GS/IC0 and +-1 for the Jacobi
+family.  Iterates are not bit-exact because dot products are reduced in a
+different order than the reference's sequential loop.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, golden_matrix
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a GPU", allow_module_level=True)
+
+import lap_gb300 as gb  # noqa: E402
+import oracle  # noqa: E402
+from lap_gb300 import gen  # noqa: E402
+
+X_TOL = 1e-6  # solution tolerance vs the reference (spec acceptance)
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def iters_ok(got, want, prec):
+    slack = 1 if prec in ("line_jacobi", "none", "it_jacobi") else max(1, int(np.ceil(0.02 * want)))
+    return abs(got - want) <= slack
+
+
+@pytest.mark.parametrize("prec", ["line_jacobi", "GS_std", "ichol", "it_jacobi", "GS_it2", "none"])
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_pcg_matches_reference(golden, name, prec):
+    n, ia, ja, a, b = golden_matrix(golden, name)
+    it, flag, M, K, maxit = (int(v) for v in golden[f"{name}_{prec}_it"])
+    tol = float(golden[f"{name}_{prec}_tol"][0])
+    xref = golden[f"{name}_{prec}_x"]
+    sysm = gb.System(dev(ia), dev(ja), dev(a), prec, M, K)
+    x, r, hist = sysm.solve(dev(b), tol=tol, maxit=maxit, hist_len=maxit + 2)
+    assert r["flag"] == flag == 0
+    assert iters_ok(r["iters"], it, prec), (r["iters"], it)
+    xs = x.cpu().numpy()
+    assert np.linalg.norm(xs - xref) / np.linalg.norm(xref) < X_TOL
+    assert hist[0] == pytest.approx(golden[f"{name}_{prec}_hist"][0], rel=1e-12)
+    assert r["res"] < tol * hist[0]
+    sysm.close()
+
+
+def test_gs_it_diverging_case_hits_maxit(golden):
+    """GS_it with M=K=1 does not converge on these inputs in the reference either."""
+    n, ia, ja, a, b = golden_matrix(golden, "grid2d")
+    it, flag, M, K, maxit = (int(v) for v in golden["grid2d_GS_it_it"])
+    sysm = gb.System(dev(ia), dev(ja), dev(a), "GS_it", M, K)
+    x, r = sysm.solve(dev(b), tol=float(golden["grid2d_GS_it_tol"][0]), maxit=maxit)
+    assert flag == 1 and r["flag"] == 1 and r["iters"] == it == maxit + 1
+    sysm.close()
+
+
+@pytest.mark.parametrize("prec", ["line_jacobi", "GS_std", "ichol"])
+def test_graph_and_eager_agree(prec):
+    A, b = gen.grid2d_unit(48, seed=11)
+    sysm = gb.System.from_csr(A, prec)
+    x1, r1 = sysm.solve(dev(b), tol=1e-9, maxit=3000, use_graph=True)
+    x2, r2 = sysm.solve(dev(b), tol=1e-9, maxit=3000, use_graph=False)
+    assert r1["iters"] == r2["iters"] and r1["flag"] == r2["flag"] == 0
+    assert torch.equal(x1, x2)  # deterministic reductions: bitwise identical
+    x3, r3 = sysm.solve(dev(b), tol=1e-9, maxit=3000)
+    assert torch.equal(x1, x3)  # and run-to-run reproducible
+    sysm.close()
+
+
+@pytest.mark.parametrize("prec", ["line_jacobi", "ichol", "GS_std"])
+def test_mixed_precision_error_vs_fp64_oracle(prec):
+    A, b = gen.grid3d_lognormal(20, seed=1002)
+    ref = oracle.solve(A.n, A.ia, A.ja, A.a, b, prec, 1e-13, 20000)
+    sysm = gb.System.from_csr(A, prec)
+    x, r = sysm.solve(dev(b), tol=1e-10, maxit=20000, precision=1)
+    assert r["flag"] == 0 and r["outer"] >= 2
+    assert r["rel_true_res"] < 1e-10 * 1.01
+    err = np.linalg.norm(x.cpu().numpy() - ref["x"]) / np.linalg.norm(ref["x"])
+    assert err < 1e-8, err
+    sysm.close()
+
+
+def test_host_buffers_solve():
+    A, b = gen.grid2d_unit(40, seed=5)
+    ref = oracle.solve(A.n, A.ia, A.ja, A.a, b, "ichol", 1e-10, 3000)
+    sysm = gb.System.from_csr(A, "ichol")
+    x, r = sysm.solve_host(b, tol=1e-10, maxit=3000)
+    assert iters_ok(r["iters"], ref["iters"], "ichol")
+    assert np.linalg.norm(x - ref["x"]) / np.linalg.norm(ref["x"]) < X_TOL
+    sysm.close()
+
+
+def test_nonzero_initial_guess():
+    A, b = gen.grid2d_unit(30, seed=9)
+    x0 = np.random.default_rng(1).standard_normal(A.n)
+    ref = oracle.solve(A.n, A.ia, A.ja, A.a, b, "GS_std", 1e-10, 3000, x0=x0)
+    sysm = gb.System.from_csr(A, "GS_std")
+    x, r = sysm.solve(dev(b), dev(x0), tol=1e-10, maxit=3000)
+    assert iters_ok(r["iters"], ref["iters"], "GS_std")
+    assert np.linalg.norm(x.cpu().numpy() - ref["x"]) / np.linalg.norm(ref["x"]) < X_TOL
+    sysm.close()
+
+
+def _pdata_gpu_convention(A, prec, keep):
+    """LAP's CUDA-driver setup (cg_driver2.c:95-144, :210-351) on the device."""
+    L_ = gb.lib()
+    n = A.n
+    Lp, Up, d = oracle.split(n, A.ia, A.ja, A.a)
+    if prec == "GS_std":
+        Lp, Up = oracle.embed_diagonal(n, Lp, Up, d)
+    p = gb.PData()
+    p.n, p.m, p.k = n, 1, 1
+    p.prec_op = prec.encode()
+    arrs = {k: dev(v) for k, v in dict(lia=Lp[0], lja=Lp[1], la=Lp[2], uia=Up[0], uja=Up[1],
+                                        ua=Up[2], d=d).items()}
+    keep.update(arrs)
+    for k in ("lia", "lja", "la", "uia", "uja", "ua", "d"):
+        setattr(p, k, gb.ptr(arrs[k]))
+    p.lnnz, p.unnz = len(Lp[1]), len(Up[1])
+    dr = torch.zeros(n, dtype=torch.float64, device="cuda")
+    L_.cuda_vector_reciprocal(n, gb.ptr(arrs["d"]), gb.ptr(dr))
+    keep["dr"] = dr
+    p.d_r = gb.ptr(dr)
+    for k in ("aux_vec1", "aux_vec2", "aux_vec3"):
+        keep[k] = torch.zeros(n, dtype=torch.float64, device="cuda")
+        setattr(p, k, gb.ptr(keep[k]))
+    return p
+
+
+@pytest.mark.parametrize("prec", ["line_jacobi", "GS_std", "ichol", "it_jacobi"])
+def test_lap_cg_dropin(golden, prec):
+    """LAP's cg() symbol on device pointers, set up the way cg_driver2.c's CUDA
+    branch does, reproduces the reference's iterations and solution."""
+    n, ia, ja, a, b = golden_matrix(golden, "grid3d")
+    it_ref, flag_ref, M, K, maxit = (int(v) for v in golden[f"grid3d_{prec}_it"])
+    tol = float(golden[f"grid3d_{prec}_tol"][0])
+    A = gen.CSR(n, ia, ja, a)
+    keep = {}
+    p = _pdata_gpu_convention(A, prec, keep)
+    p.k = K
+    dia, dja, da, db = dev(ia), dev(ja), dev(a), dev(b)
+    if prec == "ichol":
+        iv = dev(a.copy())
+        gb.lib().initialize_ichol(n, len(ja), gb.ptr(dia), gb.ptr(dja), gb.ptr(iv))
+        keep["iv"] = iv
+        p.ichol_vals = gb.ptr(iv)
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    hist = np.zeros(maxit + 3)
+    it, flag = C.c_int(), C.c_int()
+    torch.cuda.synchronize()
+    gb.lib().cg(n, float(len(ja)), gb.ptr(dia), gb.ptr(dja), gb.ptr(da), gb.ptr(x), gb.ptr(db), tol,
+                C.byref(p), maxit, C.byref(it), C.byref(flag), hist.ctypes.data)
+    assert flag.value == 0 and iters_ok(it.value, it_ref, prec)
+    xs = x.cpu().numpy()
+    xref = golden[f"grid3d_{prec}_x"]
+    assert np.linalg.norm(xs - xref) / np.linalg.norm(xref) < X_TOL
+    # prec_function applies the same preconditioner as the reference, in the
+    # reference's operation order: bit-identical to the oracle
+    y = torch.zeros(n, dtype=torch.float64, device="cuda")
+    gb.lib().prec_function(gb.ptr(dia), gb.ptr(dja), gb.ptr(da), len(ja), C.byref(p), gb.ptr(db), gb.ptr(y))
+    assert np.array_equal(y.cpu().numpy(), oracle.prec_apply(n, ia, ja, a, b, prec, 1, K))
+
+
+@pytest.mark.parametrize("prec", ["line_jacobi", "GS_std", "ichol", "it_jacobi", "GS_it", "GS_it2", "none"])
+def test_precond_apply_bit_exact(golden, prec):
+    n, ia, ja, a, b = golden_matrix(golden, "knn")
+    sysm = gb.System(dev(ia), dev(ja), dev(a), prec, 1, 2)
+    y = sysm.precond(dev(b))
+    assert np.array_equal(y.cpu().numpy(), oracle.prec_apply(n, ia, ja, a, b, prec, 1, 2))
+    sysm.close()
+
+
+def test_breakdown_on_zero_rhs():
+    A, _ = gen.grid2d_unit(16, seed=1)
+    sysm = gb.System.from_csr(A, "ichol")
+    x, r = sysm.solve(torch.zeros(A.n, dtype=torch.float64, device="cuda"), tol=1e-8, maxit=100)
+    assert r["flag"] == 2 and r["status"] == 2  # rho = p'q = 0: breakdown, not NaN
+    assert not x.any()
+    sysm.close()
+
+
+def test_bad_inputs_rejected():
+    A, _ = gen.grid2d_unit(8, seed=1)
+    rows = np.repeat(np.arange(A.n), np.diff(A.ia))
+    keep = rows != A.ja
+    keep[A.ia[3]:A.ia[4]] = True  # drop every diagonal but row 3's
+    ja2 = A.ja[keep]
+    ia2 = np.zeros(A.n + 1, dtype=np.int32)
+    np.cumsum(np.bincount(rows[keep], minlength=A.n), out=ia2[1:])
+    with pytest.raises(gb.GbError) as e:
+        gb.System(dev(ia2), dev(ja2), dev(A.a[keep]), "ichol")
+    assert e.value.status == 5
+    with pytest.raises(gb.GbError):
+        gb.System.from_csr(A, "no_such_preconditioner")
+
+
+def test_zero_pivot_reported():
+    A, b = gen.grid2d_unit(8, seed=1)
+    a = A.a.copy()
+    rows = np.repeat(np.arange(A.n), np.diff(A.ia))
+    a[(rows == A.ja) & (rows == 5)] = -1.0
+    sysm = gb.System(dev(A.ia), dev(A.ja), dev(a), "ichol")
+    assert sysm.info()["status"] == 3
+    x, r = sysm.solve(dev(b), tol=1e-8, maxit=50)
+    assert r["flag"] == 2
+    sysm.close()
+
+
+def test_sync_free_wait_timeout_reports_status():
+    """Failure path of the sync-free solves without faulting or hanging the GPU:
+    a 1 ns wait budget makes every wait that has to spin give up at its first
+    clock check; the solve must come back with GB_TIMEOUT, and the system must
+    work normally again once the default budget is restored."""
+    A, b = gen.grid2d_unit(512, seed=2)  # 1023 levels: later rows always spin
+    sysm = gb.System.from_csr(A, "GS_std")
+    gb.check(gb.lib().gb_debug_set_spin_budget(sysm.h, 1), "set budget")
+    x, r = sysm.solve(dev(b), tol=1e-8, maxit=20)
+    assert r["status"] == 4
+    gb.check(gb.lib().gb_debug_set_spin_budget(sysm.h, 0), "reset budget")
+    x, r = sysm.solve(dev(b), tol=1e-8, maxit=5000)
+    assert r["status"] == 0 and r["flag"] == 0
+    sysm.close()
+
+
+def test_large_grid3d_properties():
+    """64^3 lognormal: converges, true residual meets tol, IC0 beats Jacobi in iterations."""
+    A, b = gen.grid3d_lognormal(64, seed=1002)
+    res = {}
+    for prec in ("line_jacobi", "ichol", "GS_std"):
+        sysm = gb.System.from_csr(A, prec)
+        x, r = sysm.solve(dev(b), tol=1e-8, maxit=10000)
+        assert r["flag"] == 0 and r["rel_true_res"] < 2e-8
+        res[prec] = r["iters"]
+        sysm.close()
+    assert res["ichol"] < res["line_jacobi"] and res["GS_std"] < res["line_jacobi"]
