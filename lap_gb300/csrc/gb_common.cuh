@@ -89,14 +89,22 @@ __device__ __forceinline__ uint64_t spin_budget(const int* err) {
 // Spin until *p holds a computed value.  On timeout (or when another waiter
 // already timed out, signalled through *err) returns a quiet NaN and records
 // GB_TIMEOUT in *err.
+//
+// Backoff: __nanosleep doubling from 32 ns to kMaxSleepNs between polls, so
+// rows far ahead of the wavefront poll rarely and the L2 stays free for the
+// rows at the front.
+constexpr unsigned kMaxSleepNs = 256u;
+
 template <typename T>
 __device__ __forceinline__ T wait_value(const T* p, int* err) {
   T v = ld_relaxed(p);
   if (!is_sentinel(v)) return v;
   const uint64_t t0 = globaltimer_ns();
   const uint64_t budget = spin_budget(err);
-  unsigned polls = 0;
+  unsigned polls = 0, ns = 32u;
   while (true) {
+    __nanosleep(ns);
+    if (ns < kMaxSleepNs) ns <<= 1;
     v = ld_relaxed(p);
     if (!is_sentinel(v)) return v;
     if ((++polls & kPollCheck) == 0u) {
@@ -113,8 +121,10 @@ __device__ __forceinline__ bool wait_flag(const int* flag, int* err) {
   if (ld_acquire(flag) != 0) return true;
   const uint64_t t0 = globaltimer_ns();
   const uint64_t budget = spin_budget(err);
-  unsigned polls = 0;
+  unsigned polls = 0, ns = 32u;
   while (true) {
+    __nanosleep(ns);
+    if (ns < kMaxSleepNs) ns <<= 1;
     if (ld_acquire(flag) != 0) return true;
     if ((++polls & kPollCheck) == 0u) {
       if (ld_volatile(err) != 0 || globaltimer_ns() - t0 > budget) {

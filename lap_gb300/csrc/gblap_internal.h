@@ -49,29 +49,40 @@ struct SpmvPlan {
 };
 
 // ----------------------------------------------------------- triangular schedule
-// Rows are processed in level order (level = longest dependency chain), each
-// level padded to whole warps so a warp never waits on itself.  A warp is
-// either SHORT (32 rows, one per lane, dependencies stored column-major:
-// entry k of lane l at ptr + k*32 + l) or LONG (one row, its dependencies
-// contiguous, reduced by the whole warp).
+// Tiled level schedule of one triangular factor (see tri_kernel.cuh).  Rows
+// are cut into contiguous tiles of tile_rows rows, processed in dependency
+// order (ascending for a lower factor, descending for an upper one).  Inside
+// a tile, rows are grouped by their level among the tile's own rows, and each
+// level into 32-row slices: a SHORT slice holds one row per lane with its
+// dependencies column-major (entry k of lane l at ent + k*32 + l); a LONG
+// slice holds one row with more than 32 dependencies, contiguous, reduced by
+// a whole warp.
 struct TriPlan {
   int n = 0;
   bool lower = true;
-  int nlevels = 0;
-  int nwarps = 0;
+  int nlevels = 0;           // global dependency depth (diagnostics)
+  int tile_rows = 0;
+  int ntiles = 0;
+  int nlvl = 0;              // tile-local levels, summed over tiles
+  int nslices = 0;
   int nent = 0;
   long long ndeps = 0;       // dependencies without padding (algorithmic size)
-  int *slot_row = nullptr;   // [nwarps*32] row or -1 (LONG warps: lane 0 only)
-  int *warp_ptr = nullptr;   // [nwarps+1] entry offsets
-  int *warp_len = nullptr;   // [nwarps] deps per lane (SHORT) or deps of the row (LONG, negated)
+  int *tile_row0 = nullptr, *tile_row1 = nullptr;  // [ntiles], processing order
+  int *tile_lvl = nullptr;   // [ntiles+1]
+  int *lvl_slice = nullptr;  // [nlvl+1]
+  int *slice_rows = nullptr; // [nslices*32]
+  int *slice_ent = nullptr;  // [nslices]
+  int *slice_len = nullptr;  // [nslices]
   int *ecol = nullptr;       // [nent] dependency row, -1 padding
   int *emap = nullptr;       // [nent] index of the value in the entry source array
-  int *dmap = nullptr;       // [nwarps*32] index of the diagonal in the diagonal source array
-  double *eval = nullptr;    // [nent]
-  double *diag = nullptr;    // [nwarps*32]
-  float *eval32 = nullptr;
-  float *diag32 = nullptr;
-  unsigned *ticket = nullptr;  // dynamic block order + completion counter
+  int *dmap = nullptr;       // [nslices*32] index of the diagonal in the diagonal source
+  double *eval = nullptr, *diag = nullptr, *dinv = nullptr;
+  float *eval32 = nullptr, *diag32 = nullptr, *dinv32 = nullptr;
+  // rows in global level order, each level padded to a multiple of 32 with
+  // -1 (the IC(0) factorization walks this order)
+  int *order = nullptr;
+  int norder = 0;
+  unsigned *ticket = nullptr;  // [0] next tile, [1] finished tiles, [2] exited blocks
 };
 
 }  // namespace gb

@@ -7,6 +7,9 @@
 // The dot product is deterministic: per-block partials in a fixed grid,
 // summed in block order by the last block to finish (single launch).
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "gb_common.cuh"
@@ -27,6 +30,22 @@ int device_sm_count() {
 }
 
 int reduction_grid() { return device_sm_count() * kRedBlocksPerSM; }
+
+int occupancy_blocks(const void* kernel, int threads, size_t dyn_smem) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, int> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  const auto key = std::make_pair(kernel, threads);
+  auto f = cache.find(key);
+  if (f != cache.end()) return f->second;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, dyn_smem) != cudaSuccess || nb < 1) {
+    cudaGetLastError();
+    nb = 1;
+  }
+  cache[key] = nb;
+  return nb;
+}
 
 static int ew_grid(long long n) {
   const long long need = (n + kRedThreads - 1) / kRedThreads;
@@ -95,7 +114,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32)
   XPlain<T> xf{x};
   EpAxpby<T> ep{y, beta};
   for (int b = blockIdx.x * kSpmvWarps + wid; b < nb; b += gridDim.x * kSpmvWarps)
-    spmv_bundle(b, n, bundles, ia, ja, a, alpha, xf, ep, stage[wid]);
+    spmv_bundle<T, true>(b, n, bundles, ia, ja, a, alpha, xf, ep, stage[wid]);
 }
 
 template <typename T>
@@ -103,7 +122,7 @@ int spmv_axpby(const SpmvPlan* plan, int n, const int* ia, const int* ja, const 
                const T* x, T beta, T* y, cudaStream_t s) {
   if (n <= 0) return GB_OK;
   const int nb = plan ? plan->nbundles : ceil_div(n, 32);
-  const int blocks = std::max(1, std::min(ceil_div(nb, kSpmvWarps), device_sm_count() * 8));
+  const int blocks = wave_grid(spmv_axpby_kernel<T>, kSpmvWarps * 32, ceil_div(nb, kSpmvWarps));
   spmv_axpby_kernel<T><<<blocks, kSpmvWarps * 32, 0, s>>>(n, nb, plan ? plan->bundles : nullptr,
                                                           ia, ja, a, alpha, x, beta, y);
   GB_CUDA_TRY(cudaGetLastError());

@@ -6,6 +6,14 @@
 namespace gb {
 
 int device_sm_count();
+// Resident blocks per SM of `kernel` at this block size (cached); grids of
+// the grid-stride kernels are sized to one full wave: SMs x this.
+int occupancy_blocks(const void* kernel, int threads, size_t dyn_smem = 0);
+template <typename K>
+inline int wave_grid(K kernel, int threads, long long work_blocks) {
+  const long long cap = (long long)device_sm_count() * occupancy_blocks((const void*)kernel, threads);
+  return (int)(work_blocks < 1 ? 1 : (work_blocks < cap ? work_blocks : cap));
+}
 
 // Greedy row bundles for `rows_per_bundle` <= 32 rows and <= kBundleNnz entries.
 int spmv_plan_build(int n, int nnz, const int* ia_host, SpmvPlan* plan, int rows_per_bundle);

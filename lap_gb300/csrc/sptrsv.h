@@ -29,7 +29,14 @@ int transpose_positions(int n, const int* ia, const int* ja, std::vector<int>* t
 int deps_ichol(int n, const int* ia, const int* ja, const std::vector<int>& tpos, bool lower,
                TriDeps* d);
 
-int tri_plan_build(const TriDeps& d, TriPlan* plan);
+// tile_rows <= 0: one tile per SM for large matrices, 1024..16384 rows.
+int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows = 0);
+int tri_default_tile_rows(int n);
+// Resident CTAs per SM of the tiled solves (default 1, limited by shared
+// memory anyway); GBLAP_TRI_BLOCKS_PER_SM overrides it (1..8).
+int tri_grid(int ntiles);
+int tri_blocks_per_sm();
+void tri_set_blocks_per_sm(int bps);
 void tri_plan_free(TriPlan* plan);
 // eval/diag (and their FP32 copies when want32) from value arrays.
 int tri_plan_fill(TriPlan* plan, const double* ent_src, const double* diag_src, bool want32,

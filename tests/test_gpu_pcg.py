@@ -31,7 +31,7 @@ def dev(a):
 
 
 def iters_ok(got, want, prec):
-    slack = 1 if prec in ("line_jacobi", "none", "it_jacobi") else max(1, int(np.ceil(0.02 * want)))
+    slack = 1 if prec in ("line_jacobi", "it_jacobi") else max(1, int(np.ceil(0.02 * want)))
     return abs(got - want) <= slack
 
 
