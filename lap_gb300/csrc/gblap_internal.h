@@ -57,6 +57,23 @@ struct SpmvPlan {
 // dependencies column-major (entry k of lane l at ent + k*32 + l); a LONG
 // slice holds one row with more than 32 dependencies, contiguous, reduced by
 // a whole warp.
+// Each tile-local level is stored as one or more RECORDS (tri_kernel.cuh):
+// a 16-byte header, the rows, their diagonal and its reciprocal, and the
+// dependency columns and values column-major -- contiguous and 16-byte
+// aligned so one TMA bulk copy stages a record in shared memory.  The FP64
+// and FP32 record buffers share the row partition; their value slots are
+// written from the factor's value array through the fill maps.
+struct RecordSet {
+  unsigned char *buf = nullptr;  // records
+  long long bytes = 0;
+  long long *off = nullptr;      // [nrec] byte offset of each record
+  int *nbytes = nullptr;         // [nrec]
+  long long *vdst = nullptr;     // [nval] element index (T units) of each entry value
+  long long *ddst = nullptr;     // [ndiag] element index of each diagonal
+  long long *idst = nullptr;     // [ndiag] element index of each reciprocal
+  void *long_val = nullptr;      // [nlong] values of long rows
+};
+
 struct TriPlan {
   int n = 0;
   bool lower = true;
@@ -64,20 +81,18 @@ struct TriPlan {
   int tile_rows = 0;
   int ntiles = 0;
   int nlvl = 0;              // tile-local levels, summed over tiles
-  int nslices = 0;
-  int nent = 0;
+  int nrec = 0;
   long long ndeps = 0;       // dependencies without padding (algorithmic size)
   int *tile_row0 = nullptr, *tile_row1 = nullptr;  // [ntiles], processing order
-  int *tile_lvl = nullptr;   // [ntiles+1]
-  int *lvl_slice = nullptr;  // [nlvl+1]
-  int *slice_rows = nullptr; // [nslices*32]
-  int *slice_ent = nullptr;  // [nslices]
-  int *slice_len = nullptr;  // [nslices]
-  int *ecol = nullptr;       // [nent] dependency row, -1 padding
-  int *emap = nullptr;       // [nent] index of the value in the entry source array
-  int *dmap = nullptr;       // [nslices*32] index of the diagonal in the diagonal source
-  double *eval = nullptr, *diag = nullptr, *dinv = nullptr;
-  float *eval32 = nullptr, *diag32 = nullptr, *dinv32 = nullptr;
+  int *tile_rec = nullptr;   // [ntiles+1]
+  int *rec_flags = nullptr;  // [nrec]
+  RecordSet r64, r32;
+  int nval = 0, ndiag = 0, nlong = 0;
+  int *vsrc = nullptr;       // [nval] index of each entry value in the value source array
+  int *dsrc = nullptr;       // [ndiag] index of each diagonal in the diagonal source array
+  int *long_col = nullptr;   // [nlong]
+  int *long_src = nullptr;   // [nlong]
+  bool have32 = false;
   // rows in global level order, each level padded to a multiple of 32 with
   // -1 (the IC(0) factorization walks this order)
   int *order = nullptr;

@@ -264,15 +264,24 @@ struct OpPcgLower {
     }
     set_cond(cond, has_cond, false);
   }
-  __device__ T rhs(int i) {
-    if (!do_update) return r[i];
-    x[i] = fma_rn(a, p[i], x[i]);
-    const T ri = fma_rn(na, q[i], r[i]);
+  struct Pre {
+    T x, p, r, q;
+  };
+  struct DPre {};
+  __device__ Pre pre(int i) const {
+    if (!do_update) return {T(0), T(0), r[i], T(0)};
+    return {x[i], p[i], r[i], q[i]};
+  }
+  __device__ T rhs(int i, const Pre& v) {
+    if (!do_update) return v.r;
+    x[i] = fma_rn(a, v.p, v.x);
+    const T ri = fma_rn(na, v.q, v.r);
     r[i] = ri;
     rr += (double)ri * (double)ri;
     return ri;
   }
-  __device__ void done(int i, T) {
+  __device__ DPre dpre(int) const { return {}; }
+  __device__ void done(int i, T, const DPre&) {
     if (sfill) sfill[i] = sentinel<T>();
   }
   __device__ void chunk_end(int c, int nchunks, unsigned* ticket, double* sm) {
@@ -334,8 +343,16 @@ struct OpIcUpper {
   }
   __device__ bool active() const { return !dn; }
   __device__ void inactive_end() {}
-  __device__ T rhs(int i) const { return t[i]; }
-  __device__ void done(int i, T y) { rho += (double)r[i] * (double)y; }
+  struct Pre {
+    T t;
+  };
+  struct DPre {
+    T r;
+  };
+  __device__ Pre pre(int i) const { return {t[i]}; }
+  __device__ T rhs(int, const Pre& v) const { return v.t; }
+  __device__ DPre dpre(int i) const { return {r[i]}; }
+  __device__ void done(int, T y, const DPre& v) { rho += (double)v.r * (double)y; }
   __device__ void chunk_end(int c, int nchunks, unsigned* ticket, double* sm) {
     rho_chunk_end(rho, st, part, c, nchunks, ticket, sm);
   }
@@ -361,15 +378,24 @@ struct OpGsUpper {
   }
   __device__ bool active() const { return !dn; }
   __device__ void inactive_end() {}
-  __device__ T rhs(int i) const {
-    T acc = r[i];
-    for (int j = ia[i]; j < ia[i + 1]; ++j) acc = fma_rn(-av[j], t[ja[j]], acc);
+  struct Pre {
+    T r;
+    int j0, j1;
+  };
+  struct DPre {
+    T t, r;
+  };
+  __device__ Pre pre(int i) const { return {r[i], ia[i], ia[i + 1]}; }
+  __device__ T rhs(int, const Pre& v) const {
+    T acc = v.r;
+    for (int j = v.j0; j < v.j1; ++j) acc = fma_rn(-av[j], t[ja[j]], acc);
     return acc;
   }
-  __device__ void done(int i, T y) {
-    const T wi = t[i] + y;
+  __device__ DPre dpre(int i) const { return {t[i], r[i]}; }
+  __device__ void done(int i, T y, const DPre& v) {
+    const T wi = v.t + y;
     w[i] = wi;
-    rho += (double)r[i] * (double)wi;
+    rho += (double)v.r * (double)wi;
   }
   __device__ void chunk_end(int c, int nchunks, unsigned* ticket, double* sm) {
     rho_chunk_end(rho, st, part, c, nchunks, ticket, sm);

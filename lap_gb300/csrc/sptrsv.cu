@@ -1,14 +1,13 @@
-// sptrsv.cu -- host-side scheduling for the tiled sync-free triangular
-// solves (replacing csrsv2 analysis, cuda_blas.cu:99-224) and the on-device
-// IC(0) factorization (replacing cusparseDcsric02, cuda_blas.cu:261-488).
+// sptrsv.cu -- dependency lists of the triangular factors (host) and the
+// on-device IC(0) factorization (replacing cusparseDcsric02,
+// cuda_blas.cu:261-488).  The tiled solve schedule is in tri_plan.cu.
 #include <algorithm>
-#include <cstdlib>
 #include <vector>
 
 #include "gb_common.cuh"
 #include "kernels.h"
 #include "sptrsv.h"
-#include "tri_kernel.cuh"
+#include "spmv_bundle.cuh"
 
 namespace gb {
 
@@ -103,245 +102,6 @@ int deps_ichol(int n, const int* ia, const int* ja, const std::vector<int>& tpos
   }
   return GB_OK;
 }
-
-// ------------------------------------------------------------ schedule
-template <typename V>
-static int upload(V** dst, const std::vector<V>& src) {
-  const size_t bytes = sizeof(V) * std::max<size_t>(src.size(), 1);
-  GB_CUDA_TRY(cudaMalloc(dst, bytes));
-  if (!src.empty()) GB_CUDA_TRY(cudaMemcpy(*dst, src.data(), sizeof(V) * src.size(), cudaMemcpyHostToDevice));
-  return GB_OK;
-}
-
-int tri_default_tile_rows(int n) {
-  // one tile per SM when the matrix is large; at least 1024 rows, at most
-  // 16384 (128 KB of FP64 shared memory)
-  const int sms = device_sm_count();
-  int t = 1024;
-  while (t < 16384 && (long long)t * sms < n) t <<= 1;
-  return t;
-}
-
-int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
-  const int n = d.n;
-  const bool lower = d.lower;
-  if (tile_rows <= 0) tile_rows = tri_default_tile_rows(n);
-  tile_rows = std::max(32, std::min(tile_rows, 16384));
-  auto deps_of = [&](int r) { return d.row_ptr[r + 1] - d.row_ptr[r]; };
-
-  // global levels: the IC(0) factorization order and a diagnostic
-  std::vector<int> lev(n, 0);
-  int nlev = 0;
-  for (int q = 0; q < n; ++q) {
-    const int i = lower ? q : n - 1 - q;
-    int l = 0;
-    for (int k = d.row_ptr[i]; k < d.row_ptr[i + 1]; ++k) l = std::max(l, lev[d.dep_col[k]] + 1);
-    lev[i] = l;
-    nlev = std::max(nlev, l + 1);
-  }
-  std::vector<int> order;
-  {
-    std::vector<int> lptr(nlev + 1, 0);
-    for (int i = 0; i < n; ++i) lptr[lev[i] + 1]++;
-    for (int l = 0; l < nlev; ++l) lptr[l + 1] += lptr[l];
-    std::vector<int> byl(n), fill(lptr.begin(), lptr.end() - 1);
-    for (int i = 0; i < n; ++i) byl[fill[lev[i]]++] = i;
-    for (int l = 0; l < nlev; ++l) {
-      for (int p = lptr[l]; p < lptr[l + 1]; ++p) order.push_back(byl[p]);
-      while (order.size() % 32) order.push_back(-1);
-    }
-  }
-
-  // tiles, local levels, slices
-  const int ntiles = (n + tile_rows - 1) / tile_rows;
-  std::vector<int> tr0, tr1, tile_lvl{0}, lvl_slice{0}, slice_rows, slice_ent, slice_len, ecol, emap, dmap;
-  std::vector<int> llev(tile_rows), bucket_ptr, bucket;
-  for (int q = 0; q < ntiles; ++q) {
-    const int tix = lower ? q : ntiles - 1 - q;
-    const int t0 = tix * tile_rows, t1 = std::min(n, t0 + tile_rows);
-    tr0.push_back(t0);
-    tr1.push_back(t1);
-    int nl = 0;
-    for (int s = 0; s < t1 - t0; ++s) {
-      const int i = lower ? t0 + s : t1 - 1 - s;
-      int l = 0;
-      for (int k = d.row_ptr[i]; k < d.row_ptr[i + 1]; ++k) {
-        const int c = d.dep_col[k];
-        if (c >= t0 && c < t1) l = std::max(l, llev[c - t0] + 1);
-      }
-      llev[i - t0] = l;
-      nl = std::max(nl, l + 1);
-    }
-    bucket_ptr.assign(nl + 1, 0);
-    for (int i = t0; i < t1; ++i) bucket_ptr[llev[i - t0] + 1]++;
-    for (int l = 0; l < nl; ++l) bucket_ptr[l + 1] += bucket_ptr[l];
-    bucket.resize(t1 - t0);
-    std::vector<int> fill(bucket_ptr.begin(), bucket_ptr.end() - 1);
-    for (int i = t0; i < t1; ++i) bucket[fill[llev[i - t0]]++] = i;
-    for (int l = 0; l < nl; ++l) {
-      std::vector<int> shortrows, longrows;
-      for (int p = bucket_ptr[l]; p < bucket_ptr[l + 1]; ++p)
-        (deps_of(bucket[p]) > 32 ? longrows : shortrows).push_back(bucket[p]);
-      for (size_t s0 = 0; s0 < shortrows.size(); s0 += 32) {
-        const int cnt = (int)std::min<size_t>(32, shortrows.size() - s0);
-        int len = 0;
-        for (int t = 0; t < cnt; ++t) len = std::max(len, deps_of(shortrows[s0 + t]));
-        const int base = (int)ecol.size();
-        ecol.resize(base + (size_t)len * 32, -1);
-        emap.resize(base + (size_t)len * 32, -1);
-        for (int t = 0; t < 32; ++t) {
-          const int r = t < cnt ? shortrows[s0 + t] : -1;
-          slice_rows.push_back(r);
-          dmap.push_back(r >= 0 ? d.diag_src[r] : -1);
-          if (r < 0) continue;
-          for (int k = d.row_ptr[r], e = 0; k < d.row_ptr[r + 1]; ++k, ++e) {
-            ecol[base + e * 32 + t] = d.dep_col[k];
-            emap[base + e * 32 + t] = d.dep_src[k];
-          }
-        }
-        slice_ent.push_back(base);
-        slice_len.push_back(len);
-      }
-      for (int r : longrows) {
-        slice_ent.push_back((int)ecol.size());
-        slice_len.push_back(-deps_of(r));
-        for (int k = d.row_ptr[r]; k < d.row_ptr[r + 1]; ++k) {
-          ecol.push_back(d.dep_col[k]);
-          emap.push_back(d.dep_src[k]);
-        }
-        slice_rows.push_back(r);
-        dmap.push_back(d.diag_src[r]);
-        for (int t = 1; t < 32; ++t) {
-          slice_rows.push_back(-1);
-          dmap.push_back(-1);
-        }
-      }
-      lvl_slice.push_back((int)slice_len.size());
-    }
-    tile_lvl.push_back((int)lvl_slice.size() - 1);
-  }
-  plan->n = n;
-  plan->lower = lower;
-  plan->nlevels = nlev;
-  plan->tile_rows = tile_rows;
-  plan->ntiles = ntiles;
-  plan->nlvl = (int)lvl_slice.size() - 1;
-  plan->nslices = (int)slice_len.size();
-  plan->nent = (int)ecol.size();
-  plan->ndeps = (long long)d.dep_col.size();
-  plan->norder = (int)order.size();
-  GB_TRY(upload(&plan->tile_row0, tr0));
-  GB_TRY(upload(&plan->tile_row1, tr1));
-  GB_TRY(upload(&plan->tile_lvl, tile_lvl));
-  GB_TRY(upload(&plan->lvl_slice, lvl_slice));
-  GB_TRY(upload(&plan->slice_rows, slice_rows));
-  GB_TRY(upload(&plan->slice_ent, slice_ent));
-  GB_TRY(upload(&plan->slice_len, slice_len));
-  GB_TRY(upload(&plan->ecol, ecol));
-  GB_TRY(upload(&plan->emap, emap));
-  GB_TRY(upload(&plan->dmap, dmap));
-  GB_TRY(upload(&plan->order, order));
-  GB_CUDA_TRY(cudaMalloc(&plan->eval, sizeof(double) * std::max(1, plan->nent)));
-  GB_CUDA_TRY(cudaMalloc(&plan->diag, sizeof(double) * std::max(1, plan->nslices * 32)));
-  GB_CUDA_TRY(cudaMalloc(&plan->dinv, sizeof(double) * std::max(1, plan->nslices * 32)));
-  GB_CUDA_TRY(cudaMalloc(&plan->ticket, sizeof(unsigned) * 4));
-  GB_CUDA_TRY(cudaMemset(plan->ticket, 0, sizeof(unsigned) * 4));
-  return GB_OK;
-}
-
-void tri_plan_free(TriPlan* p) {
-  void* ptrs[] = {p->tile_row0, p->tile_row1, p->tile_lvl, p->lvl_slice, p->slice_rows,
-                  p->slice_ent, p->slice_len, p->ecol,     p->emap,      p->dmap,
-                  p->eval,      p->diag,      p->dinv,     p->eval32,    p->diag32,
-                  p->dinv32,    p->order,     p->ticket};
-  for (void* q : ptrs)
-    if (q) cudaFree(q);
-  *p = TriPlan();
-}
-
-__global__ void recip_kernel(int n, const double* __restrict__ d, double* r, float* r32) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const double v = d[i] != 0.0 ? 1.0 / d[i] : 0.0;
-    r[i] = v;
-    if (r32) r32[i] = (float)v;
-  }
-}
-
-int tri_plan_fill(TriPlan* p, const double* ent_src, const double* diag_src, bool want32,
-                  cudaStream_t s) {
-  const int nd = p->nslices * 32;
-  if (want32 && !p->eval32) {
-    GB_CUDA_TRY(cudaMalloc(&p->eval32, sizeof(float) * std::max(1, p->nent)));
-    GB_CUDA_TRY(cudaMalloc(&p->diag32, sizeof(float) * std::max(1, nd)));
-    GB_CUDA_TRY(cudaMalloc(&p->dinv32, sizeof(float) * std::max(1, nd)));
-  }
-  GB_TRY(gather_values(p->nent, p->emap, ent_src, p->eval, want32 ? p->eval32 : nullptr, s));
-  GB_TRY(gather_values(nd, p->dmap, diag_src, p->diag, want32 ? p->diag32 : nullptr, s));
-  if (nd > 0) {
-    recip_kernel<<<std::max(1, std::min(device_sm_count() * 8, ceil_div(nd, 256))), 256, 0, s>>>(
-        nd, p->diag, p->dinv, want32 ? p->dinv32 : nullptr);
-    GB_CUDA_TRY(cudaGetLastError());
-  }
-  return GB_OK;
-}
-
-// ------------------------------------------------------------ launching
-static int g_tri_bps = 0;
-
-int tri_blocks_per_sm() {
-  if (g_tri_bps == 0) {
-    const char* e = getenv("GBLAP_TRI_BLOCKS_PER_SM");
-    const int v = e ? atoi(e) : 0;
-    g_tri_bps = (v >= 1 && v <= 8) ? v : 1;
-  }
-  return g_tri_bps;
-}
-
-void tri_set_blocks_per_sm(int bps) { g_tri_bps = std::max(1, std::min(8, bps)); }
-
-int tri_grid(int ntiles) {
-  return std::max(1, std::min(ntiles, device_sm_count() * tri_blocks_per_sm()));
-}
-
-template <typename T>
-TriArgs<T> tri_args(const TriPlan& p, T* y, int* err) {
-  TriArgs<T> A;
-  A.ntiles = p.ntiles;
-  A.tile_row0 = p.tile_row0;
-  A.tile_row1 = p.tile_row1;
-  A.tile_lvl = p.tile_lvl;
-  A.lvl_slice = p.lvl_slice;
-  A.slice_rows = p.slice_rows;
-  A.slice_ent = p.slice_ent;
-  A.slice_len = p.slice_len;
-  A.ecol = p.ecol;
-  if constexpr (sizeof(T) == 8) {
-    A.eval = (const T*)p.eval;
-    A.diag = (const T*)p.diag;
-    A.dinv = (const T*)p.dinv;
-  } else {
-    A.eval = (const T*)p.eval32;
-    A.diag = (const T*)p.diag32;
-    A.dinv = (const T*)p.dinv32;
-  }
-  A.y = y;
-  A.ticket = p.ticket;
-  A.err = err;
-  A.lower = p.lower ? 1 : 0;
-  return A;
-}
-template TriArgs<double> tri_args<double>(const TriPlan&, double*, int*);
-template TriArgs<float> tri_args<float>(const TriPlan&, float*, int*);
-
-template <typename T>
-int tri_solve_plain(const TriPlan* p, const T* x, T* y, int* err, cudaStream_t s) {
-  if (p->n <= 0) return GB_OK;
-  GB_TRY(fill_sentinel_dev(p->n, y, s));
-  OpPlain<T> op{x};
-  return tri_launch<T, OpPlain<T>, true>(*p, tri_args<T>(*p, y, err), op, s);
-}
-template int tri_solve_plain<double>(const TriPlan*, const double*, double*, int*, cudaStream_t);
-template int tri_solve_plain<float>(const TriPlan*, const float*, float*, int*, cudaStream_t);
 
 // ------------------------------------------------------------ IC(0) factor
 // Left-looking restatement of simple_blas.c:139-168: row j receives, for

@@ -1,4 +1,4 @@
-// tri_kernel.cuh -- tiled sync-free sparse triangular solve.
+// tri_kernel.cuh -- tiled sync-free sparse triangular solve, TMA-staged.
 //
 // Replaces cusparseDcsrsv2_solve (cuda_blas.cu:731-820, :500, :516).  Every
 // row is solved as simple_lower/upper_triangular_solve (simple_blas.c:46-85)
@@ -9,21 +9,24 @@
 // dependency chain counts.
 //
 // Schedule (TriPlan, built on the host): rows are cut into contiguous tiles;
-// inside a tile, rows are grouped by their level with respect to the tile's
-// own rows, and each level into 32-row slices (entries column-major).  One
-// CTA solves one tile at a time, holding the tile's values in shared memory:
-//   A) rhs of every row into shared memory      (coalesced, tile-wide)
-//   B) level by level: each warp solves slices of the level; a dependency
-//      inside the tile is read from shared memory (ready after the previous
-//      level's barrier), one in an earlier tile is read from global memory,
-//      spinning on the producer's value (outputs are pre-filled with a
-//      sentinel) with __nanosleep backoff; results go to shared memory and
-//      global memory; __syncthreads between levels
+// inside a tile rows are grouped by their level with respect to the tile's
+// own rows; each level is stored as one or more contiguous, 16-byte aligned
+// RECORDS (rows, diagonal, reciprocal, dependency columns and values,
+// column-major).  One CTA solves one tile at a time:
+//   A) rhs of every row into shared memory (coalesced, tile-wide);
+//   B) a producer warp streams the tile's records into a ring of shared
+//      memory slots with cp.async.bulk (TMA), signalling an mbarrier per
+//      slot; four consumer warps take the records in order: a dependency
+//      inside the tile is read from shared memory (written at an earlier
+//      level, ordered by a named barrier between levels), one in an earlier
+//      tile from global memory by spinning on the producer's value (outputs
+//      are pre-filled with a sentinel); results go to shared memory and
+//      global memory;
 //   C) per-row epilogue (fused vector updates, dot partials), coalesced.
-// The next level's slice (indices, values, first remote values) is loaded
-// before each barrier, so the dependency chain does not wait on DRAM.
 // Tiles are taken by ticket in dependency order by a persistent grid, so a
-// tile only ever waits on tiles already being solved by running CTAs.
+// tile only waits on tiles already being solved by running CTAs.  Every
+// wait (mbarrier or value) is bounded in wall-clock time; on expiry the
+// error word is set and the CTA drains its own copies before leaving.
 //
 // OP contract:
 //   void begin();  bool active();  void inactive_end()   (block 0, !active)
@@ -39,27 +42,36 @@
 
 namespace gb {
 
-constexpr int kTriThreads = 128;  // 4 warps per CTA
-constexpr int kTriPrefetch = 8;   // dependencies held in registers per row
+constexpr int kTriConsumers = 4;                       // consumer warps
+constexpr int kTriThreads = (kTriConsumers + 1) * 32;  // + one producer warp
+constexpr int kTriSlots = 4;                           // ring depth
+constexpr int kTriSlotBytes = 16384;                   // max record size
+constexpr int kRecLong = 2;                            // record flag: one row, warp-reduced
+constexpr int kRecBarrier = 1;                         // record flag: level ends here
+
+// Record header (16 bytes).  Layout after it, R4 = nrows rounded up to 4:
+//   int rows[R4]; T diag[R4]; T dinv[R4]; int cols[len*R4]; T vals[len*R4]
+// (LONG records: no cols/vals; they live at long_col/long_val[off ...]).
+struct RecHdr {
+  int nrows, len, flags, off;
+};
 
 template <typename T>
 struct TriArgs {
   int ntiles;
-  const int* __restrict__ tile_row0;   // [ntiles] first row (processing order)
-  const int* __restrict__ tile_row1;   // [ntiles] one past the last row
-  const int* __restrict__ tile_lvl;    // [ntiles+1] level range of each tile
-  const int* __restrict__ lvl_slice;   // [nlevels_total+1] slice range of each level
-  const int* __restrict__ slice_rows;  // [nslices*32] row or -1
-  const int* __restrict__ slice_ent;   // [nslices] entry offset
-  const int* __restrict__ slice_len;   // [nslices] deps per lane, or -deps of a long row
-  const int* __restrict__ ecol;        // [nent] dependency row or -1
-  const T* __restrict__ eval;
-  const T* __restrict__ diag;          // [nslices*32]
-  const T* __restrict__ dinv;          // [nslices*32] 1/diag
+  const int* __restrict__ tile_row0;  // [ntiles] first row (processing order)
+  const int* __restrict__ tile_row1;  // [ntiles] one past the last row
+  const int* __restrict__ tile_rec;   // [ntiles+1] record range of each tile
+  const long long* __restrict__ rec_off;  // [nrec] byte offset in recbuf
+  const int* __restrict__ rec_bytes;      // [nrec]
+  const int* __restrict__ rec_flags;      // [nrec] kRecBarrier / kRecLong
+  const unsigned char* __restrict__ recbuf;
+  const int* __restrict__ long_col;
+  const T* __restrict__ long_val;
   T* y;              // output, pre-filled with the sentinel
   unsigned* ticket;  // [0] next tile, [1] finished tiles, [2] exited blocks
   int* err;
-  int lower;
+  int tile_rows;
 };
 
 __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
@@ -72,95 +84,149 @@ __device__ __forceinline__ bool chunk_finished(unsigned* ticket, int nchunks) {
   return atomicAdd(&ticket[1], 1u) == (unsigned)nchunks - 1u;
 }
 
-// One slice's registers: a row per lane and its first kTriPrefetch deps.
-template <typename T>
-struct SliceRegs {
-  int row, len, base;
-  int cols[kTriPrefetch];
-  T vals[kTriPrefetch];
-  T rem[kTriPrefetch];  // early-read remote values (may still be the sentinel)
-  T dg;
-};
-
-template <typename T>
-__device__ __forceinline__ void load_slice(const TriArgs<T>& A, int s, int lane, int t0, int t1,
-                                           SliceRegs<T>& R, bool exact) {
-  R.len = __ldg(A.slice_len + s);
-  R.base = __ldg(A.slice_ent + s);
-  R.row = __ldg(A.slice_rows + s * 32 + lane);
-  if (R.len < 0 || R.row < 0) return;
-  R.dg = exact ? __ldg(A.diag + s * 32 + lane) : __ldg(A.dinv + s * 32 + lane);
-#pragma unroll
-  for (int k = 0; k < kTriPrefetch; ++k) {
-    R.cols[k] = -1;
-    if (k < R.len) {
-      const int c = __ldg(A.ecol + R.base + k * 32 + lane);
-      R.cols[k] = c;
-      R.vals[k] = __ldg(A.eval + R.base + k * 32 + lane);
-      if (c >= 0 && (c < t0 || c >= t1)) R.rem[k] = ld_relaxed(A.y + c);
+// ------------------------------------------------------------ mbarrier / TMA
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait on an mbarrier phase; false on timeout / abort.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity, int* err) {
+  if (mbar_try_wait(b, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  const uint64_t budget = spin_budget(err);
+  while (true) {
+    if (mbar_try_wait(b, parity)) return true;
+    if (ld_volatile(err) != 0 || globaltimer_ns() - t0 > budget) {
+      atomicCAS(err, 0, (int)GB_TIMEOUT);
+      return false;
     }
   }
 }
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void named_barrier_consumers() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kTriConsumers * 32) : "memory");
+}
 
 template <typename T>
-__device__ __forceinline__ T dep_value(const TriArgs<T>& A, const T* sm, int c, int t0, int t1,
-                                       T early) {
+__device__ __forceinline__ T dep_value(const T* y, const T* sm, int c, int t0, int t1, int* err) {
   if (c >= t0 && c < t1) return sm[c - t0];
-  if (!is_sentinel(early)) return early;
-  return wait_value(A.y + c, A.err);
+  return wait_value(y + c, err);
 }
 
+// Solves the rows of one staged record (consumer threads ct = 0..127).
 template <typename T, bool EXACT>
-__device__ __forceinline__ void solve_slice(const TriArgs<T>& A, T* sm, int t0, int t1,
-                                            const SliceRegs<T>& R, int lane) {
-  if (R.row < 0) return;
-  T acc = sm[R.row - t0];
-#pragma unroll
-  for (int k = 0; k < kTriPrefetch; ++k) {
-    const int c = R.cols[k];
-    if (c >= 0) {
-      const T v = dep_value(A, sm, c, t0, t1, R.rem[k]);
-      acc = EXACT ? sub_rn(acc, mul_rn(R.vals[k], v)) : fma_rn(-R.vals[k], v, acc);
+__device__ __forceinline__ void solve_record(const TriArgs<T>& A, T* sm, int t0, int t1,
+                                             const unsigned char* rec, int ct) {
+  const RecHdr h = *reinterpret_cast<const RecHdr*>(rec);
+  const int R4 = (h.nrows + 3) & ~3;
+  const int* rows = reinterpret_cast<const int*>(rec + sizeof(RecHdr));
+  const T* diag = reinterpret_cast<const T*>(rows + R4);
+  const T* dinv = diag + R4;
+  if (h.flags & kRecLong) {
+    // one row, the whole first consumer warp reduces it
+    if (ct >= 32) return;
+    const int row = rows[0];
+    T acc = T(0);
+    for (int k = ct; k < h.len; k += 32) {
+      const int c = __ldg(A.long_col + h.off + k);
+      acc = fma_rn(__ldg(A.long_val + h.off + k), dep_value(A.y, sm, c, t0, t1, A.err), acc);
     }
+    acc = warp_sum(acc);
+    if (ct == 0) {
+      const T r = sub_rn(sm[row - t0], acc);
+      const T yv = publishable(EXACT ? div_rn(r, diag[0]) : r * dinv[0]);
+      sm[row - t0] = yv;
+      st_relaxed(A.y + row, yv);
+    }
+    return;
   }
-  for (int k = kTriPrefetch; k < R.len; ++k) {
-    const int c = __ldg(A.ecol + R.base + k * 32 + lane);
-    if (c < 0) break;
-    const T l = __ldg(A.eval + R.base + k * 32 + lane);
-    const T v = dep_value(A, sm, c, t0, t1, sentinel<T>());
-    acc = EXACT ? sub_rn(acc, mul_rn(l, v)) : fma_rn(-l, v, acc);
-  }
-  const T yv = publishable(EXACT ? div_rn(acc, R.dg) : acc * R.dg);
-  sm[R.row - t0] = yv;
-  st_relaxed(A.y + R.row, yv);
-}
-
-// A row with more than 32 dependencies: the whole warp reduces it.
-template <typename T, bool EXACT>
-__device__ __forceinline__ void solve_long(const TriArgs<T>& A, T* sm, int t0, int t1, int s,
-                                           int lane) {
-  const int row = __ldg(A.slice_rows + s * 32);
-  const int cnt = -__ldg(A.slice_len + s);
-  const int base = __ldg(A.slice_ent + s);
-  T acc = T(0);
-  for (int k = lane; k < cnt; k += 32) {
-    const int c = __ldg(A.ecol + base + k);
-    const T v = dep_value(A, sm, c, t0, t1, sentinel<T>());
-    acc = add_rn(acc, mul_rn(__ldg(A.eval + base + k), v));
-  }
-  acc = warp_sum(acc);
-  if (lane == 0) {
-    const T r = sub_rn(sm[row - t0], acc);
-    const T yv = publishable(EXACT ? div_rn(r, __ldg(A.diag + s * 32)) : r * __ldg(A.dinv + s * 32));
+  const int* cols = reinterpret_cast<const int*>(dinv + R4);
+  const T* vals = reinterpret_cast<const T*>(cols + (size_t)h.len * R4);
+  for (int r = ct; r < h.nrows; r += kTriConsumers * 32) {
+    const int row = rows[r];
+    T acc = sm[row - t0];
+    for (int k = 0; k < h.len; ++k) {
+      const int c = cols[k * R4 + r];
+      if (c < 0) break;
+      const T l = vals[k * R4 + r];
+      const T v = dep_value(A.y, sm, c, t0, t1, A.err);
+      acc = EXACT ? sub_rn(acc, mul_rn(l, v)) : fma_rn(-l, v, acc);
+    }
+    const T yv = publishable(EXACT ? div_rn(acc, diag[r]) : acc * dinv[r]);
     sm[row - t0] = yv;
     st_relaxed(A.y + row, yv);
   }
 }
 
+// Phase A / C loops: every thread first issues the loads of kTriUnroll rows
+// (OP::pre / OP::dpre), then computes and stores them, so a tile's vector
+// traffic streams instead of paying one DRAM round trip per row.
+constexpr int kTriUnroll = 8;
+
+template <typename T, typename OP>
+__device__ __forceinline__ void phase_rhs(OP& op, T* sm, int t0, int t1) {
+  for (int b = t0 + (int)threadIdx.x; b < t1; b += kTriUnroll * kTriThreads) {
+    typename OP::Pre pr[kTriUnroll];
+#pragma unroll
+    for (int u = 0; u < kTriUnroll; ++u) {
+      const int i = b + u * kTriThreads;
+      if (i < t1) pr[u] = op.pre(i);
+    }
+#pragma unroll
+    for (int u = 0; u < kTriUnroll; ++u) {
+      const int i = b + u * kTriThreads;
+      if (i < t1) sm[i - t0] = op.rhs(i, pr[u]);
+    }
+  }
+}
+
+template <typename T, typename OP>
+__device__ __forceinline__ void phase_done(OP& op, const T* sm, int t0, int t1) {
+  for (int b = t0 + (int)threadIdx.x; b < t1; b += kTriUnroll * kTriThreads) {
+    typename OP::DPre pr[kTriUnroll];
+#pragma unroll
+    for (int u = 0; u < kTriUnroll; ++u) {
+      const int i = b + u * kTriThreads;
+      if (i < t1) pr[u] = op.dpre(i);
+    }
+#pragma unroll
+    for (int u = 0; u < kTriUnroll; ++u) {
+      const int i = b + u * kTriThreads;
+      if (i < t1) op.done(i, sm[i - t0], pr[u]);
+    }
+  }
+}
+
 template <typename T, typename OP, bool EXACT>
 __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP op) {
-  extern __shared__ __align__(16) unsigned char tri_smem[];
-  T* sm = reinterpret_cast<T*>(tri_smem);
+  extern __shared__ __align__(128) unsigned char tri_smem[];
+  unsigned char* ring = tri_smem;                                   // kTriSlots x kTriSlotBytes
+  T* sm = reinterpret_cast<T*>(tri_smem + kTriSlots * kTriSlotBytes);  // tile values
+  __shared__ __align__(8) uint64_t full_bar[kTriSlots], empty_bar[kTriSlots];
   __shared__ int s_tile;
   __shared__ double s_red[64];
   op.begin();
@@ -168,8 +234,19 @@ __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP 
     if (blockIdx.x == 0 && threadIdx.x == 0) op.inactive_end();
     return;  // no ticket touched
   }
-  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  constexpr int W = kTriThreads / 32;
+  const int wid = threadIdx.x >> 5;
+  const bool producer = wid == kTriConsumers;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kTriSlots; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], kTriConsumers);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  unsigned issued = 0;    // records issued by this CTA's producer (all tiles)
+  unsigned consumed = 0;  // records consumed by this CTA's consumers
+  bool failed = false;
   while (true) {
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(&A.ticket[0], 1u);
     __syncthreads();
@@ -177,42 +254,65 @@ __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP 
     __syncthreads();
     if (k >= A.ntiles) break;
     const int t0 = __ldg(A.tile_row0 + k), t1 = __ldg(A.tile_row1 + k);
+    const int rec0 = __ldg(A.tile_rec + k), rec1 = __ldg(A.tile_rec + k + 1);
     // A) right-hand sides
-    for (int i = t0 + threadIdx.x; i < t1; i += kTriThreads) sm[i - t0] = op.rhs(i);
-    const int l0 = __ldg(A.tile_lvl + k), l1 = __ldg(A.tile_lvl + k + 1);
-    SliceRegs<T> R;
-    bool have = false;
-    if (l0 < l1) {
-      const int s = __ldg(A.lvl_slice + l0) + wid;
-      if (s < __ldg(A.lvl_slice + l0 + 1)) {
-        load_slice(A, s, lane, t0, t1, R, EXACT);
-        have = true;
+    phase_rhs<T>(op, sm, t0, t1);
+    __syncthreads();
+    // B) records
+    if (producer) {
+      if ((threadIdx.x & 31) == 0) {
+        for (int j = rec0; j < rec1 && !failed; ++j, ++issued) {
+          const int slot = issued % kTriSlots;
+          const unsigned use = issued / kTriSlots;
+          if (!mbar_wait(&empty_bar[slot], (use & 1u) ^ 1u, A.err)) {
+            failed = true;
+            break;
+          }
+          const unsigned bytes = (unsigned)__ldg(A.rec_bytes + j);
+          mbar_expect_tx(&full_bar[slot], bytes);
+          tma_load_1d(ring + slot * kTriSlotBytes, A.recbuf + __ldg(A.rec_off + j), bytes,
+                      &full_bar[slot]);
+        }
+      }
+      issued = __shfl_sync(0xffffffffu, issued, 0);
+      failed = __shfl_sync(0xffffffffu, failed, 0);
+    } else {
+      const int ct = threadIdx.x;
+      for (int j = rec0; j < rec1; ++j, ++consumed) {
+        const int slot = consumed % kTriSlots;
+        const unsigned use = consumed / kTriSlots;
+        if (!failed && !mbar_wait(&full_bar[slot], use & 1u, A.err)) failed = true;
+        const unsigned char* rec = ring + slot * kTriSlotBytes;
+        if (!failed) {
+          solve_record<T, EXACT>(A, sm, t0, t1, rec, ct);
+        }
+        __syncwarp();
+        if ((ct & 31) == 0) mbar_arrive(&empty_bar[slot]);
+        // level ends: read from global so every consumer warp takes the same
+        // barriers even if one of them gave up waiting for a record
+        if (__ldg(A.rec_flags + j) & kRecBarrier) named_barrier_consumers();
       }
     }
     __syncthreads();
-    // B) levels of the tile
-    for (int lv = l0; lv < l1; ++lv) {
-      const int s0 = __ldg(A.lvl_slice + lv), s1 = __ldg(A.lvl_slice + lv + 1);
-      for (int s = s0 + wid; s < s1; s += W) {
-        if (!have) load_slice(A, s, lane, t0, t1, R, EXACT);
-        have = false;
-        if (R.len < 0) solve_long<T, EXACT>(A, sm, t0, t1, s, lane);
-        else solve_slice<T, EXACT>(A, sm, t0, t1, R, lane);
-      }
-      if (lv + 1 < l1) {
-        const int sn = s1 + wid;  // this warp's first slice of the next level
-        if (sn < __ldg(A.lvl_slice + lv + 2)) {
-          load_slice(A, sn, lane, t0, t1, R, EXACT);
-          have = true;
-        }
-      }
-      __syncthreads();
-    }
     // C) epilogue
-    for (int i = t0 + threadIdx.x; i < t1; i += kTriThreads) op.done(i, sm[i - t0]);
+    phase_done<T>(op, sm, t0, t1);
     op.chunk_end(k, A.ntiles, A.ticket, s_red);
     __syncthreads();
   }
+  // Drain: every issued copy has been consumed (consumers wait on each full
+  // barrier, or fail only after the error word is set; in that case wait,
+  // bounded, for the copies still in flight before the CTA's shared memory
+  // goes away).
+  if (threadIdx.x == 0) {
+    for (unsigned u = consumed; u < issued; ++u) {
+      const int slot = u % kTriSlots;
+      const uint64_t t0 = globaltimer_ns();
+      while (!mbar_try_wait(&full_bar[slot], (u / kTriSlots) & 1u) &&
+             globaltimer_ns() - t0 < kSpinBudgetNs) {
+      }
+    }
+  }
+  __syncthreads();
   // the last block to leave resets the counters for the next launch
   if (threadIdx.x == 0) {
     __threadfence();
@@ -227,16 +327,16 @@ __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP 
 
 int tri_blocks_per_sm();
 
-// Launches the tiled solve: dynamic shared memory = one tile of T values; a
-// persistent grid of min(tiles, SMs x resident CTAs) blocks.
+// Launches the tiled solve: dynamic shared memory = the record ring plus one
+// tile of T values; a persistent grid of min(tiles, SMs x resident CTAs).
 template <typename T, typename OP, bool EXACT>
 int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   if (p.ntiles <= 0) return GB_OK;
-  const size_t smem = (size_t)p.tile_rows * sizeof(T);
+  const size_t smem = (size_t)kTriSlots * kTriSlotBytes + (size_t)p.tile_rows * sizeof(T);
   static bool attr_set = false;  // one per instantiation
   if (!attr_set) {
     GB_CUDA_TRY(cudaFuncSetAttribute(tri_tile_kernel<T, OP, EXACT>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr_set = true;
   }
   int per_sm = 0;
@@ -261,11 +361,17 @@ TriArgs<T> tri_args(const TriPlan& p, T* y, int* err);
 template <typename T>
 struct OpPlain {
   const T* __restrict__ x;
+  struct Pre {
+    T x;
+  };
+  struct DPre {};
   __device__ __forceinline__ void begin() {}
   __device__ __forceinline__ bool active() const { return true; }
   __device__ __forceinline__ void inactive_end() {}
-  __device__ __forceinline__ T rhs(int r) const { return x[r]; }
-  __device__ __forceinline__ void done(int, T) {}
+  __device__ __forceinline__ Pre pre(int r) const { return {x[r]}; }
+  __device__ __forceinline__ T rhs(int, const Pre& p) const { return p.x; }
+  __device__ __forceinline__ DPre dpre(int) const { return {}; }
+  __device__ __forceinline__ void done(int, T, const DPre&) {}
   __device__ __forceinline__ void chunk_end(int, int nchunks, unsigned* ticket, double*) {
     if (threadIdx.x == 0) chunk_finished(ticket, nchunks);
   }

@@ -1,0 +1,359 @@
+// tri_plan.cu -- tiled record schedule of a triangular factor (replacing the
+// csrsv2 analysis of cuda_blas.cu:99-224) and its launchers.
+#include <algorithm>
+#include <cstdlib>
+#include <vector>
+
+#include "gb_common.cuh"
+#include "kernels.h"
+#include "sptrsv.h"
+#include "tri_kernel.cuh"
+
+namespace gb {
+
+template <typename V>
+static int upload(V** dst, const std::vector<V>& src) {
+  const size_t bytes = sizeof(V) * std::max<size_t>(src.size(), 1);
+  GB_CUDA_TRY(cudaMalloc(dst, bytes));
+  if (!src.empty()) GB_CUDA_TRY(cudaMemcpy(*dst, src.data(), sizeof(V) * src.size(), cudaMemcpyHostToDevice));
+  return GB_OK;
+}
+
+int tri_default_tile_rows(int n) {
+  // one tile per SM when the matrix is large; at least 1024 rows, at most
+  // 16384 (128 KB of FP64 shared memory beside the 64 KB record ring)
+  const int sms = device_sm_count();
+  int t = 1024;
+  while (t < 16384 && (long long)t * sms < n) t <<= 1;
+  return t;
+}
+
+namespace {
+
+constexpr int kLongDeps = 64;  // rows with more dependencies get a LONG record
+
+inline long long align16(long long b) { return (b + 15) & ~15LL; }
+
+// bytes of a SHORT record with `rows` rows of up to `len` dependencies
+inline long long rec_size(int rows, int len, int S) {
+  const long long R4 = (rows + 3) & ~3;
+  return 16 + 4 * R4 + 2LL * S * R4 + (long long)len * R4 * (4 + S);
+}
+
+struct RecDesc {
+  int tile_level_end;  // 1 when this record closes its level
+  bool is_long;
+  int len;
+  std::vector<int> rows;
+};
+
+// Lays out all records in precision S; fills the RecordSet's host images.
+void layout(const TriDeps& d, const std::vector<RecDesc>& recs, int S, std::vector<unsigned char>& buf,
+            std::vector<long long>& off, std::vector<int>& nbytes, std::vector<long long>& vdst,
+            std::vector<long long>& ddst, std::vector<long long>& idst,
+            std::vector<int>* vsrc, std::vector<int>* dsrc, std::vector<int>* long_col,
+            std::vector<int>* long_src) {
+  buf.clear();
+  off.clear();
+  nbytes.clear();
+  vdst.clear();
+  ddst.clear();
+  idst.clear();
+  for (const RecDesc& r : recs) {
+    const int nrows = (int)r.rows.size();
+    const long long R4 = (nrows + 3) & ~3;
+    const long long bytes = r.is_long ? rec_size(nrows, 0, S) : rec_size(nrows, r.len, S);
+    const long long base = (long long)buf.size();
+    off.push_back(base);
+    nbytes.push_back((int)bytes);
+    buf.resize(base + bytes, 0);
+    int* hdr = reinterpret_cast<int*>(buf.data() + base);
+    hdr[0] = nrows;
+    hdr[1] = r.len;
+    hdr[2] = (r.tile_level_end ? kRecBarrier : 0) | (r.is_long ? kRecLong : 0);
+    hdr[3] = 0;
+    int* rows = hdr + 4;
+    for (long long t = 0; t < R4; ++t) rows[t] = t < nrows ? r.rows[t] : -1;
+    const long long diag_el = (base + 16 + 4 * R4) / S;  // element index of diag[0]
+    for (int t = 0; t < nrows; ++t) {
+      ddst.push_back(diag_el + t);
+      idst.push_back(diag_el + R4 + t);
+      if (dsrc) dsrc->push_back(d.diag_src[r.rows[t]]);
+    }
+    if (r.is_long) {
+      const int row = r.rows[0];
+      hdr[3] = long_col ? (int)long_col->size() : 0;
+      if (long_col)
+        for (int k = d.row_ptr[row]; k < d.row_ptr[row + 1]; ++k) {
+          long_col->push_back(d.dep_col[k]);
+          long_src->push_back(d.dep_src[k]);
+        }
+      continue;
+    }
+    int* cols = reinterpret_cast<int*>(buf.data() + base + 16 + 4 * R4 + 2 * S * R4);
+    const long long vals_el = (base + 16 + 4 * R4 + 2 * S * R4 + 4LL * r.len * R4) / S;
+    for (long long q = 0; q < (long long)r.len * R4; ++q) cols[q] = -1;
+    for (int t = 0; t < nrows; ++t) {
+      const int row = r.rows[t];
+      for (int k = d.row_ptr[row], e = 0; k < d.row_ptr[row + 1]; ++k, ++e) {
+        cols[e * R4 + t] = d.dep_col[k];
+        vdst.push_back(vals_el + e * R4 + t);
+        if (vsrc) vsrc->push_back(d.dep_src[k]);
+      }
+    }
+  }
+}
+
+int upload_set(RecordSet* rs, const std::vector<unsigned char>& buf, const std::vector<long long>& off,
+               const std::vector<int>& nbytes, const std::vector<long long>& vdst,
+               const std::vector<long long>& ddst, const std::vector<long long>& idst, size_t nlong,
+               size_t S) {
+  rs->bytes = (long long)buf.size();
+  GB_TRY(upload(&rs->buf, buf));
+  GB_TRY(upload(&rs->off, off));
+  GB_TRY(upload(&rs->nbytes, nbytes));
+  GB_TRY(upload(&rs->vdst, vdst));
+  GB_TRY(upload(&rs->ddst, ddst));
+  GB_TRY(upload(&rs->idst, idst));
+  GB_CUDA_TRY(cudaMalloc(&rs->long_val, S * std::max<size_t>(nlong, 1)));
+  return GB_OK;
+}
+
+void free_set(RecordSet* rs) {
+  void* p[] = {rs->buf, rs->off, rs->nbytes, rs->vdst, rs->ddst, rs->idst, rs->long_val};
+  for (void* q : p)
+    if (q) cudaFree(q);
+  *rs = RecordSet();
+}
+
+}  // namespace
+
+int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
+  const int n = d.n;
+  const bool lower = d.lower;
+  if (tile_rows <= 0) tile_rows = tri_default_tile_rows(n);
+  tile_rows = std::max(32, std::min(tile_rows, 16384));
+  auto deps_of = [&](int r) { return d.row_ptr[r + 1] - d.row_ptr[r]; };
+
+  // global levels: the IC(0) factorization order and a diagnostic
+  std::vector<int> lev(n, 0);
+  int nlev = 0;
+  for (int q = 0; q < n; ++q) {
+    const int i = lower ? q : n - 1 - q;
+    int l = 0;
+    for (int k = d.row_ptr[i]; k < d.row_ptr[i + 1]; ++k) l = std::max(l, lev[d.dep_col[k]] + 1);
+    lev[i] = l;
+    nlev = std::max(nlev, l + 1);
+  }
+  std::vector<int> order;
+  {
+    std::vector<int> lptr(nlev + 1, 0);
+    for (int i = 0; i < n; ++i) lptr[lev[i] + 1]++;
+    for (int l = 0; l < nlev; ++l) lptr[l + 1] += lptr[l];
+    std::vector<int> byl(n), fill(lptr.begin(), lptr.end() - 1);
+    for (int i = 0; i < n; ++i) byl[fill[lev[i]]++] = i;
+    for (int l = 0; l < nlev; ++l) {
+      for (int p = lptr[l]; p < lptr[l + 1]; ++p) order.push_back(byl[p]);
+      while (order.size() % 32) order.push_back(-1);
+    }
+  }
+
+  // tiles -> tile-local levels -> records
+  const int ntiles = (n + tile_rows - 1) / tile_rows;
+  std::vector<int> tr0, tr1, tile_rec{0}, rec_flags;
+  std::vector<RecDesc> recs;
+  std::vector<int> llev(tile_rows), bptr, bucket;
+  int nlvl = 0;
+  for (int q = 0; q < ntiles; ++q) {
+    const int tix = lower ? q : ntiles - 1 - q;
+    const int t0 = tix * tile_rows, t1 = std::min(n, t0 + tile_rows);
+    tr0.push_back(t0);
+    tr1.push_back(t1);
+    int nl = 0;
+    for (int s = 0; s < t1 - t0; ++s) {
+      const int i = lower ? t0 + s : t1 - 1 - s;
+      int l = 0;
+      for (int k = d.row_ptr[i]; k < d.row_ptr[i + 1]; ++k) {
+        const int c = d.dep_col[k];
+        if (c >= t0 && c < t1) l = std::max(l, llev[c - t0] + 1);
+      }
+      llev[i - t0] = l;
+      nl = std::max(nl, l + 1);
+    }
+    nlvl += nl;
+    bptr.assign(nl + 1, 0);
+    for (int i = t0; i < t1; ++i) bptr[llev[i - t0] + 1]++;
+    for (int l = 0; l < nl; ++l) bptr[l + 1] += bptr[l];
+    bucket.resize(t1 - t0);
+    std::vector<int> fill(bptr.begin(), bptr.end() - 1);
+    for (int i = t0; i < t1; ++i) bucket[fill[llev[i - t0]]++] = i;
+    for (int l = 0; l < nl; ++l) {
+      std::vector<int> rows(bucket.begin() + bptr[l], bucket.begin() + bptr[l + 1]);
+      // longest first, so records group rows of similar length
+      std::stable_sort(rows.begin(), rows.end(), [&](int a, int b) { return deps_of(a) > deps_of(b); });
+      const size_t first_rec = recs.size();
+      size_t p = 0;
+      while (p < rows.size() && deps_of(rows[p]) > kLongDeps) {
+        RecDesc r;
+        r.tile_level_end = 0;
+        r.is_long = true;
+        r.len = deps_of(rows[p]);
+        r.rows = {rows[p]};
+        recs.push_back(r);
+        ++p;
+      }
+      while (p < rows.size()) {
+        RecDesc r;
+        r.tile_level_end = 0;
+        r.is_long = false;
+        r.len = deps_of(rows[p]);
+        while (p < rows.size() && rec_size((int)r.rows.size() + 1, r.len, 8) <= kTriSlotBytes) {
+          r.rows.push_back(rows[p]);
+          ++p;
+        }
+        recs.push_back(r);
+      }
+      if (recs.size() > first_rec) recs.back().tile_level_end = 1;
+    }
+    tile_rec.push_back((int)recs.size());
+  }
+  for (const RecDesc& r : recs) rec_flags.push_back((r.tile_level_end ? kRecBarrier : 0) | (r.is_long ? kRecLong : 0));
+
+  std::vector<unsigned char> buf;
+  std::vector<long long> off, vdst, ddst, idst;
+  std::vector<int> nbytes, vsrc, dsrc, long_col, long_src;
+  layout(d, recs, 8, buf, off, nbytes, vdst, ddst, idst, &vsrc, &dsrc, &long_col, &long_src);
+  plan->nval = (int)vsrc.size();
+  plan->ndiag = (int)dsrc.size();
+  plan->nlong = (int)long_col.size();
+  GB_TRY(upload_set(&plan->r64, buf, off, nbytes, vdst, ddst, idst, long_col.size(), 8));
+  {
+    // same record order, so the FP32 pass yields the same value/long order
+    std::vector<int> vs2, ds2, lc2, ls2;
+    layout(d, recs, 4, buf, off, nbytes, vdst, ddst, idst, &vs2, &ds2, &lc2, &ls2);
+  }
+  GB_TRY(upload_set(&plan->r32, buf, off, nbytes, vdst, ddst, idst, long_col.size(), 4));
+
+  plan->n = n;
+  plan->lower = lower;
+  plan->nlevels = nlev;
+  plan->tile_rows = tile_rows;
+  plan->ntiles = ntiles;
+  plan->nlvl = nlvl;
+  plan->nrec = (int)recs.size();
+  plan->ndeps = (long long)d.dep_col.size();
+  plan->norder = (int)order.size();
+  GB_TRY(upload(&plan->tile_row0, tr0));
+  GB_TRY(upload(&plan->tile_row1, tr1));
+  GB_TRY(upload(&plan->tile_rec, tile_rec));
+  GB_TRY(upload(&plan->rec_flags, rec_flags));
+  GB_TRY(upload(&plan->vsrc, vsrc));
+  GB_TRY(upload(&plan->dsrc, dsrc));
+  GB_TRY(upload(&plan->long_col, long_col));
+  GB_TRY(upload(&plan->long_src, long_src));
+  GB_TRY(upload(&plan->order, order));
+  GB_CUDA_TRY(cudaMalloc(&plan->ticket, sizeof(unsigned) * 4));
+  GB_CUDA_TRY(cudaMemset(plan->ticket, 0, sizeof(unsigned) * 4));
+  return GB_OK;
+}
+
+void tri_plan_free(TriPlan* p) {
+  free_set(&p->r64);
+  free_set(&p->r32);
+  void* ptrs[] = {p->tile_row0, p->tile_row1, p->tile_rec, p->rec_flags, p->vsrc,
+                  p->dsrc,      p->long_col,  p->long_src, p->order,     p->ticket};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  *p = TriPlan();
+}
+
+// Writes the factor's values into the record buffers (FP64 and, when asked,
+// FP32): entries, diagonals and their reciprocals, long-row values.
+template <typename T>
+__global__ void fill_records_kernel(int nval, const long long* __restrict__ vdst,
+                                    const int* __restrict__ vsrc, const double* __restrict__ ent,
+                                    int ndiag, const long long* __restrict__ ddst,
+                                    const long long* __restrict__ idst, const int* __restrict__ dsrc,
+                                    const double* __restrict__ dg, int nlong,
+                                    const int* __restrict__ lsrc, T* buf, T* lval) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nval; i += stride) buf[vdst[i]] = (T)ent[vsrc[i]];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ndiag; i += stride) {
+    const double v = dg[dsrc[i]];
+    buf[ddst[i]] = (T)v;
+    buf[idst[i]] = (T)(v != 0.0 ? 1.0 / v : 0.0);
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nlong; i += stride) lval[i] = (T)ent[lsrc[i]];
+}
+
+int tri_plan_fill(TriPlan* p, const double* ent_src, const double* diag_src, bool want32,
+                  cudaStream_t s) {
+  const int g = std::max(1, std::min(device_sm_count() * 8, ceil_div(std::max(p->nval, p->ndiag), 256)));
+  fill_records_kernel<double><<<g, 256, 0, s>>>(p->nval, p->r64.vdst, p->vsrc, ent_src, p->ndiag,
+                                                p->r64.ddst, p->r64.idst, p->dsrc, diag_src,
+                                                p->nlong, p->long_src, (double*)p->r64.buf,
+                                                (double*)p->r64.long_val);
+  GB_CUDA_TRY(cudaGetLastError());
+  if (want32) {
+    fill_records_kernel<float><<<g, 256, 0, s>>>(p->nval, p->r32.vdst, p->vsrc, ent_src, p->ndiag,
+                                                 p->r32.ddst, p->r32.idst, p->dsrc, diag_src,
+                                                 p->nlong, p->long_src, (float*)p->r32.buf,
+                                                 (float*)p->r32.long_val);
+    GB_CUDA_TRY(cudaGetLastError());
+    p->have32 = true;
+  }
+  return GB_OK;
+}
+
+// ------------------------------------------------------------ launching
+static int g_tri_bps = 0;
+
+int tri_blocks_per_sm() {
+  if (g_tri_bps == 0) {
+    const char* e = getenv("GBLAP_TRI_BLOCKS_PER_SM");
+    const int v = e ? atoi(e) : 0;
+    g_tri_bps = (v >= 1 && v <= 8) ? v : 1;
+  }
+  return g_tri_bps;
+}
+
+void tri_set_blocks_per_sm(int bps) { g_tri_bps = std::max(1, std::min(8, bps)); }
+
+int tri_grid(int ntiles) {
+  return std::max(1, std::min(ntiles, device_sm_count() * tri_blocks_per_sm()));
+}
+
+template <typename T>
+TriArgs<T> tri_args(const TriPlan& p, T* y, int* err) {
+  const RecordSet& rs = sizeof(T) == 8 ? p.r64 : p.r32;
+  TriArgs<T> A;
+  A.ntiles = p.ntiles;
+  A.tile_row0 = p.tile_row0;
+  A.tile_row1 = p.tile_row1;
+  A.tile_rec = p.tile_rec;
+  A.rec_off = rs.off;
+  A.rec_bytes = rs.nbytes;
+  A.rec_flags = p.rec_flags;
+  A.recbuf = rs.buf;
+  A.long_col = p.long_col;
+  A.long_val = (const T*)rs.long_val;
+  A.y = y;
+  A.ticket = p.ticket;
+  A.err = err;
+  A.tile_rows = p.tile_rows;
+  return A;
+}
+template TriArgs<double> tri_args<double>(const TriPlan&, double*, int*);
+template TriArgs<float> tri_args<float>(const TriPlan&, float*, int*);
+
+template <typename T>
+int tri_solve_plain(const TriPlan* p, const T* x, T* y, int* err, cudaStream_t s) {
+  if (p->n <= 0) return GB_OK;
+  GB_TRY(fill_sentinel_dev(p->n, y, s));
+  OpPlain<T> op{x};
+  return tri_launch<T, OpPlain<T>, true>(*p, tri_args<T>(*p, y, err), op, s);
+}
+template int tri_solve_plain<double>(const TriPlan*, const double*, double*, int*, cudaStream_t);
+template int tri_solve_plain<float>(const TriPlan*, const float*, float*, int*, cudaStream_t);
+
+}  // namespace gb
