@@ -103,8 +103,12 @@ __device__ __forceinline__ T wait_value(const T* p, int* err) {
   const uint64_t budget = spin_budget(err);
   unsigned polls = 0, ns = 32u;
   while (true) {
-    __nanosleep(ns);
-    if (ns < kMaxSleepNs) ns <<= 1;
+    // the first polls spin (a value on the critical path usually lands
+    // within a few L2 round trips), later ones back off
+    if (polls >= 16u) {
+      __nanosleep(ns);
+      if (ns < kMaxSleepNs) ns <<= 1;
+    }
     v = ld_relaxed(p);
     if (!is_sentinel(v)) return v;
     if ((++polls & kPollCheck) == 0u) {

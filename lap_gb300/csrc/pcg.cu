@@ -483,6 +483,41 @@ __global__ void add_correction_kernel(int n, double* x, const float* __restrict_
     x[i] += (double)d[i];
 }
 
+// Residual replacement (mixed precision): after r was replaced by the FP64
+// true residual, the paused FP32 recurrence resumes -- p, q, rho_prev and the
+// iteration count are kept; the pause threshold moves to delta*||r||.
+__global__ void resume_kernel(PcgState* st, const PcgState* so, double delta) {
+  st->done = 0;
+  st->flag = 1;
+  st->status = GB_OK;
+  st->spare_guard = 0;
+  st->body_count = 0;
+  st->tolrel = delta * sqrt(so->rr);
+}
+
+// Jacobi / none after a residual replacement: w = D^-1 r, rho rolled.
+template <typename T, int WK>
+__global__ void __launch_bounds__(kThreads)
+    refresh_kernel(int n, const T* __restrict__ r, T* w, const T* __restrict__ d_r, PcgState* st,
+                   double* part) {
+  __shared__ double sm[kThreads / 32];
+  double acc[1] = {0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const T ri = r[i];
+    if (WK == WK_JACOBI) {
+      const T wi = d_r[i] * ri;
+      w[i] = wi;
+      acc[0] += (double)ri * (double)wi;
+    } else {
+      acc[0] += (double)ri * (double)ri;
+    }
+  }
+  if (reduce_last<1>(acc, part, gridDim.x, blockIdx.x, &st->tk[TK_RHO], sm) && threadIdx.x == 0) {
+    st->rho_prev = st->rho;
+    st->rho = acc[0];
+  }
+}
+
 // ================================================================ host side
 // One full wave of the bundle kernels (their occupancy is set by the staging
 // buffer, kThreads/32 x kBundleNnz x sizeof(T)).
@@ -692,6 +727,30 @@ int launch_outer_resid(gb_system sys, const double* b, const double* x, int firs
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
+
+template <typename T>
+int launch_resume(gb_system sys, PcgState* st, double delta) {
+  resume_kernel<<<1, 1, 0, sys->s>>>(st, sys->st_out, delta);
+  GB_CUDA_TRY(cudaGetLastError());
+  auto v = vecs<T>(sys);
+  if (prec_fused_tri(sys->prec, sys->k)) {
+    // w = M^-1 r for the replaced r; the upper solve rolls rho
+    GB_TRY(launch_lower<T>(sys, st, 0, 0, 0));
+    return launch_upper<T>(sys, st);
+  }
+  const int wk = prec_wkind(sys->prec, sys->k);
+  if (wk == WK_PREC) return GB_NOT_SUPPORTED;
+  if (wk == WK_JACOBI)
+    refresh_kernel<T, WK_JACOBI><<<grid_ew(sys->n), kThreads, 0, sys->s>>>(
+        sys->n, v.r, v.w, dr_vals<T>(sys), st, sys->part);
+  else
+    refresh_kernel<T, WK_NONE><<<grid_ew(sys->n), kThreads, 0, sys->s>>>(
+        sys->n, v.r, v.w, dr_vals<T>(sys), st, sys->part);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
+template int launch_resume<float>(gb_system, PcgState*, double);
+template int launch_resume<double>(gb_system, PcgState*, double);
 
 int launch_add_correction(gb_system sys, double* x) {
   add_correction_kernel<<<grid_ew(sys->n), kThreads, 0, sys->s>>>(sys->n, x, sys->v32.x);

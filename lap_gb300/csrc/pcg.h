@@ -19,6 +19,11 @@ int launch_body(gb_system sys, PcgState* st, cudaGraphConditionalHandle cond, in
 int launch_true_resid(gb_system sys, const double* b, const double* x, double* out2);
 int launch_outer_resid(gb_system sys, const double* b, const double* x, int first);
 int launch_add_correction(gb_system sys, double* x);
+// Resumes a paused recurrence after its residual was replaced (mixed
+// precision): clears the pause, sets the next pause threshold to
+// delta*||r_true|| and recomputes w = M^-1 r and rho for the new r.
+template <typename T>
+int launch_resume(gb_system sys, PcgState* st, double delta);
 
 // LAP's preconditioners that are compositions of SpMV / BLAS-1 calls
 // (it_jacobi.c, GS.c GS_it / GS_it2, GS_std with k > 1, and line_jacobi /

@@ -385,11 +385,20 @@ static int get_loop_graph(gb_system s, int idx, LoopGraph** out) {
 
 // Runs one PCG recurrence on the system stream: prologue, then the loop.
 template <typename T>
+static int run_loop(gb_system s, int maxit, int use_graph);
+
+template <typename T>
 static int run_recurrence(gb_system s, double tol, int maxit, int x_zero, const T* b, int use_graph) {
-  const int idx = sizeof(T) == 8 ? 0 : 1;
   init_state_host(s->st_host, tol, maxit, s->hist_cap);
   GB_CUDA_TRY(cudaMemcpyAsync(s->st, s->st_host, sizeof(PcgState), cudaMemcpyHostToDevice, s->s));
   GB_TRY(launch_prologue<T>(s, s->st, x_zero, b));
+  return run_loop<T>(s, maxit, use_graph);
+}
+
+// Runs (or resumes) the iteration loop until the recurrence's done flag.
+template <typename T>
+static int run_loop(gb_system s, int maxit, int use_graph) {
+  const int idx = sizeof(T) == 8 ? 0 : 1;
   if (use_graph) {
     LoopGraph* lg = nullptr;
     GB_TRY(get_loop_graph<T>(s, idx, &lg));
@@ -439,30 +448,47 @@ static int solve_internal(gb_system s, const gb_pcg_opts* o, gb_pcg_result* res,
     PcgState* ho = s->st_host + 1;
     init_state_host(ho, o->tol, o->maxit, 0);
     GB_CUDA_TRY(cudaMemcpyAsync(s->st_out, ho, sizeof(PcgState), cudaMemcpyHostToDevice, s->s));
+    // One FP32 PCG recurrence with residual replacement: it pauses whenever
+    // its recursive residual has dropped by inner_tol since the last
+    // replacement; the pause folds the FP32 correction into the FP64 x,
+    // recomputes r = b - A x in FP64 (the refinement step), replaces the
+    // FP32 residual with it and resumes with p, rho and the iteration count
+    // intact -- no Krylov restart, so the iteration count stays close to the
+    // FP64 PCG's.  Convergence is judged on the FP64 residual only.
     int total = 0, outer = 0, flag = 1, status = GB_MAXIT;
     double last_res = 0.0;
-    for (;;) {
-      GB_TRY(launch_outer_resid(s, s->b_int, s->v64.x, outer == 0));
-      GB_TRY(read_state(s, ho, s->st_out));
-      last_res = std::sqrt(ho->rr);
-      if (hist_host && outer < hist_len) hist_host[outer] = last_res;
-      if (ho->done) {
-        flag = ho->flag;
-        status = ho->status;
-        break;
+    GB_TRY(launch_outer_resid(s, s->b_int, s->v64.x, 1));
+    GB_TRY(read_state(s, ho, s->st_out));
+    last_res = std::sqrt(ho->rr);
+    if (hist_host && hist_len > 0) hist_host[0] = last_res;
+    if (ho->done) {
+      flag = ho->flag;
+      status = ho->status;
+    } else {
+      GB_TRY(run_recurrence<float>(s, o->inner_tol, o->maxit, 1, s->v32.r, o->use_graph));
+      for (;;) {
+        GB_TRY(read_state(s, hs, s->st));
+        total = hs->iter;
+        if (hs->status == GB_BREAKDOWN) {
+          flag = 2;
+          status = GB_BREAKDOWN;
+          break;
+        }
+        GB_TRY(launch_add_correction(s, s->v64.x));
+        GB_TRY(launch_outer_resid(s, s->b_int, s->v64.x, 0));  // also zeroes the FP32 x
+        GB_TRY(read_state(s, ho, s->st_out));
+        ++outer;
+        last_res = std::sqrt(ho->rr);
+        if (hist_host && outer < hist_len) hist_host[outer] = last_res;
+        if (ho->done) {
+          flag = ho->flag;
+          status = ho->status;
+          break;
+        }
+        if (hs->flag == 1 || outer >= o->max_outer) break;  // out of iterations
+        GB_TRY(launch_resume<float>(s, s->st, o->inner_tol));
+        GB_TRY(run_loop<float>(s, o->maxit, o->use_graph));
       }
-      if (outer >= o->max_outer || total > o->maxit) break;
-      const int budget = std::max(1, o->maxit - total);
-      GB_TRY(run_recurrence<float>(s, o->inner_tol, budget, 1, s->v32.r, o->use_graph));
-      GB_TRY(read_state(s, hs, s->st));
-      total += hs->iter;
-      if (hs->status == GB_BREAKDOWN && hs->iter <= 1) {
-        flag = 2;
-        status = GB_BREAKDOWN;
-        break;
-      }
-      GB_TRY(launch_add_correction(s, s->v64.x));
-      ++outer;
     }
     r.iters = total;
     r.outer = outer;

@@ -137,10 +137,41 @@ __device__ __forceinline__ T dep_value(const T* y, const T* sm, int c, int t0, i
   return wait_value(y + c, err);
 }
 
+// Remote values of a thread's first row in the next record, read before the
+// level barrier so that the dependency chain does not wait on L2.
+constexpr int kTriPrefetchRemote = 2;
+template <typename T>
+struct RemotePrefetch {
+  int col[kTriPrefetchRemote];
+  T val[kTriPrefetchRemote];
+};
+
+template <typename T>
+__device__ __forceinline__ void prefetch_remote(const TriArgs<T>& A, const unsigned char* rec, int t0,
+                                                int t1, int ct, RemotePrefetch<T>& pf) {
+#pragma unroll
+  for (int q = 0; q < kTriPrefetchRemote; ++q) pf.col[q] = -1;
+  const RecHdr h = *reinterpret_cast<const RecHdr*>(rec);
+  if ((h.flags & kRecLong) || ct >= h.nrows) return;
+  const int R4 = (h.nrows + 3) & ~3;
+  const int* cols = reinterpret_cast<const int*>(rec + sizeof(RecHdr) + 4 * R4 + 2 * sizeof(T) * R4);
+  int q = 0;
+  for (int k = 0; k < h.len && q < kTriPrefetchRemote; ++k) {
+    const int c = cols[k * R4 + ct];
+    if (c < 0) break;
+    if (c < t0 || c >= t1) {
+      pf.col[q] = c;
+      pf.val[q] = ld_relaxed(A.y + c);
+      ++q;
+    }
+  }
+}
+
 // Solves the rows of one staged record (consumer threads ct = 0..127).
 template <typename T, bool EXACT>
 __device__ __forceinline__ void solve_record(const TriArgs<T>& A, T* sm, int t0, int t1,
-                                             const unsigned char* rec, int ct) {
+                                             const unsigned char* rec, int ct,
+                                             const RemotePrefetch<T>& pf) {
   const RecHdr h = *reinterpret_cast<const RecHdr*>(rec);
   const int R4 = (h.nrows + 3) & ~3;
   const int* rows = reinterpret_cast<const int*>(rec + sizeof(RecHdr));
@@ -173,7 +204,18 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, T* sm, int t0,
       const int c = cols[k * R4 + r];
       if (c < 0) break;
       const T l = vals[k * R4 + r];
-      const T v = dep_value(A.y, sm, c, t0, t1, A.err);
+      T v;
+      if (c >= t0 && c < t1) {
+        v = sm[c - t0];
+      } else {
+        v = sentinel<T>();
+        if (r == ct) {
+#pragma unroll
+          for (int q = 0; q < kTriPrefetchRemote; ++q)
+            if (pf.col[q] == c) v = pf.val[q];
+        }
+        if (is_sentinel(v)) v = wait_value(A.y + c, A.err);
+      }
       acc = EXACT ? sub_rn(acc, mul_rn(l, v)) : fma_rn(-l, v, acc);
     }
     const T yv = publishable(EXACT ? div_rn(acc, diag[r]) : acc * dinv[r]);
@@ -278,16 +320,30 @@ __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP 
       failed = __shfl_sync(0xffffffffu, failed, 0);
     } else {
       const int ct = threadIdx.x;
+      RemotePrefetch<T> pf;
+#pragma unroll
+      for (int q = 0; q < kTriPrefetchRemote; ++q) pf.col[q] = -1;
       for (int j = rec0; j < rec1; ++j, ++consumed) {
         const int slot = consumed % kTriSlots;
         const unsigned use = consumed / kTriSlots;
         if (!failed && !mbar_wait(&full_bar[slot], use & 1u, A.err)) failed = true;
         const unsigned char* rec = ring + slot * kTriSlotBytes;
         if (!failed) {
-          solve_record<T, EXACT>(A, sm, t0, t1, rec, ct);
+          solve_record<T, EXACT>(A, sm, t0, t1, rec, ct, pf);
         }
         __syncwarp();
         if ((ct & 31) == 0) mbar_arrive(&empty_bar[slot]);
+        // the next record is normally staged already: read its remote values
+        // now, before the level barrier
+#pragma unroll
+        for (int q = 0; q < kTriPrefetchRemote; ++q) pf.col[q] = -1;
+        if (!failed && j + 1 < rec1) {
+          const unsigned nx = consumed + 1;
+          if (mbar_wait(&full_bar[nx % kTriSlots], (nx / kTriSlots) & 1u, A.err))
+            prefetch_remote(A, ring + (nx % kTriSlots) * kTriSlotBytes, t0, t1, ct, pf);
+          else
+            failed = true;
+        }
         // level ends: read from global so every consumer warp takes the same
         // barriers even if one of them gave up waiting for a record
         if (__ldg(A.rec_flags + j) & kRecBarrier) named_barrier_consumers();
