@@ -44,8 +44,9 @@ namespace gb {
 
 constexpr int kTriConsumers = 4;                       // consumer warps
 constexpr int kTriThreads = (kTriConsumers + 1) * 32;  // + one producer warp
-constexpr int kTriSlots = 4;                           // ring depth
-constexpr int kTriSlotBytes = 16384;                   // max record size
+constexpr int kTriSlots = 16;                          // ring depth (records in flight)
+constexpr int kTriSlotBytes = 4096;                    // max record size
+constexpr int kTriRecTable = 1024;                     // records of a tile cached in smem
 constexpr int kRecLong = 2;                            // record flag: one row, warp-reduced
 constexpr int kRecBarrier = 1;                         // record flag: level ends here
 
@@ -269,6 +270,10 @@ __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP 
   unsigned char* ring = tri_smem;                                   // kTriSlots x kTriSlotBytes
   T* sm = reinterpret_cast<T*>(tri_smem + kTriSlots * kTriSlotBytes);  // tile values
   __shared__ __align__(8) uint64_t full_bar[kTriSlots], empty_bar[kTriSlots];
+  __shared__ long long s_roff[kTriRecTable];
+  __shared__ int s_rbytes[kTriRecTable];
+  __shared__ int s_rflags[kTriRecTable];
+  __shared__ unsigned s_issued, s_consumed;
   __shared__ int s_tile;
   __shared__ double s_red[64];
   op.begin();
@@ -297,6 +302,12 @@ __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP 
     if (k >= A.ntiles) break;
     const int t0 = __ldg(A.tile_row0 + k), t1 = __ldg(A.tile_row1 + k);
     const int rec0 = __ldg(A.tile_rec + k), rec1 = __ldg(A.tile_rec + k + 1);
+    // the tile's record table, so the producer issues copies back to back
+    for (int q = threadIdx.x; q < rec1 - rec0 && q < kTriRecTable; q += kTriThreads) {
+      s_roff[q] = __ldg(A.rec_off + rec0 + q);
+      s_rbytes[q] = __ldg(A.rec_bytes + rec0 + q);
+      s_rflags[q] = __ldg(A.rec_flags + rec0 + q);
+    }
     // A) right-hand sides
     phase_rhs<T>(op, sm, t0, t1);
     __syncthreads();
@@ -310,10 +321,11 @@ __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP 
             failed = true;
             break;
           }
-          const unsigned bytes = (unsigned)__ldg(A.rec_bytes + j);
+          const int q = j - rec0;
+          const unsigned bytes = (unsigned)(q < kTriRecTable ? s_rbytes[q] : __ldg(A.rec_bytes + j));
+          const long long off = q < kTriRecTable ? s_roff[q] : __ldg(A.rec_off + j);
           mbar_expect_tx(&full_bar[slot], bytes);
-          tma_load_1d(ring + slot * kTriSlotBytes, A.recbuf + __ldg(A.rec_off + j), bytes,
-                      &full_bar[slot]);
+          tma_load_1d(ring + slot * kTriSlotBytes, A.recbuf + off, bytes, &full_bar[slot]);
         }
       }
       issued = __shfl_sync(0xffffffffu, issued, 0);
@@ -333,20 +345,20 @@ __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP 
         }
         __syncwarp();
         if ((ct & 31) == 0) mbar_arrive(&empty_bar[slot]);
-        // the next record is normally staged already: read its remote values
-        // now, before the level barrier
+        // if the next record is staged already, read its remote values now,
+        // before the level barrier (never wait for it here)
 #pragma unroll
         for (int q = 0; q < kTriPrefetchRemote; ++q) pf.col[q] = -1;
         if (!failed && j + 1 < rec1) {
           const unsigned nx = consumed + 1;
-          if (mbar_wait(&full_bar[nx % kTriSlots], (nx / kTriSlots) & 1u, A.err))
+          if (mbar_try_wait(&full_bar[nx % kTriSlots], (nx / kTriSlots) & 1u))
             prefetch_remote(A, ring + (nx % kTriSlots) * kTriSlotBytes, t0, t1, ct, pf);
-          else
-            failed = true;
         }
-        // level ends: read from global so every consumer warp takes the same
-        // barriers even if one of them gave up waiting for a record
-        if (__ldg(A.rec_flags + j) & kRecBarrier) named_barrier_consumers();
+        // level ends: every consumer warp reads the same table, so all take
+        // the same barriers even if one of them gave up waiting for a record
+        const int q = j - rec0;
+        const int fl = q < kTriRecTable ? s_rflags[q] : __ldg(A.rec_flags + j);
+        if (fl & kRecBarrier) named_barrier_consumers();
       }
     }
     __syncthreads();
@@ -359,8 +371,11 @@ __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP 
   // barrier, or fail only after the error word is set; in that case wait,
   // bounded, for the copies still in flight before the CTA's shared memory
   // goes away).
+  if (threadIdx.x == 0) s_consumed = consumed;
+  if (threadIdx.x == kTriConsumers * 32) s_issued = issued;
+  __syncthreads();
   if (threadIdx.x == 0) {
-    for (unsigned u = consumed; u < issued; ++u) {
+    for (unsigned u = s_consumed; u < s_issued; ++u) {
       const int slot = u % kTriSlots;
       const uint64_t t0 = globaltimer_ns();
       while (!mbar_try_wait(&full_bar[slot], (u / kTriSlots) & 1u) &&

@@ -20,6 +20,11 @@ static int upload(V** dst, const std::vector<V>& src) {
 }
 
 int tri_default_tile_rows(int n) {
+  // GBLAP_TRI_TILE_ROWS overrides (32..16384; the autotuner's knob)
+  if (const char* e = getenv("GBLAP_TRI_TILE_ROWS")) {
+    const int v = atoi(e);
+    if (v >= 32 && v <= 16384) return v;
+  }
   // one tile per SM when the matrix is large; at least 1024 rows, at most
   // 16384 (128 KB of FP64 shared memory beside the 64 KB record ring)
   const int sms = device_sm_count();
@@ -207,6 +212,7 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
         r.tile_level_end = 0;
         r.is_long = false;
         r.len = deps_of(rows[p]);
+        r.rows.push_back(rows[p++]);  // a SHORT row (<= kLongDeps deps) always fits a slot
         while (p < rows.size() && rec_size((int)r.rows.size() + 1, r.len, 8) <= kTriSlotBytes) {
           r.rows.push_back(rows[p]);
           ++p;
