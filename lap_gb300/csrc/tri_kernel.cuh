@@ -9,29 +9,32 @@
 // dependency chain counts.
 //
 // Schedule (TriPlan, built on the host): rows are cut into contiguous tiles;
-// inside a tile rows are grouped by their level with respect to the tile's
-// own rows; each level is stored as one or more contiguous, 16-byte aligned
-// RECORDS (rows, diagonal, reciprocal, dependency columns and values,
-// column-major).  One CTA solves one tile at a time:
-//   A) rhs of every row into shared memory (coalesced, tile-wide);
-//   B) a producer warp streams the tile's records into a ring of shared
-//      memory slots with cp.async.bulk (TMA), signalling an mbarrier per
-//      slot; four consumer warps take the records in order: a dependency
-//      inside the tile is read from shared memory (written at an earlier
-//      level, ordered by a named barrier between levels), one in an earlier
-//      tile from global memory by spinning on the producer's value (outputs
-//      are pre-filled with a sentinel); results go to shared memory and
-//      global memory;
-//   C) per-row epilogue (fused vector updates, dot partials), coalesced.
-// Tiles are taken by ticket in dependency order by a persistent grid, so a
-// tile only waits on tiles already being solved by running CTAs.  Every
-// wait (mbarrier or value) is bounded in wall-clock time; on expiry the
-// error word is set and the CTA drains its own copies before leaving.
+// inside a tile rows are ordered by their level with respect to the tile's
+// own rows and packed into RECORDS of at most 32 rows of one level (rows,
+// diagonal, its reciprocal, dependency columns and values column-major;
+// contiguous and 16-byte aligned).  One CTA solves one tile at a time:
+//   * a producer warp streams the tile's records, in order, into a ring of
+//     shared-memory slots with cp.async.bulk (TMA), one mbarrier per slot;
+//   * consumer warps take the records round-robin, one row per lane.  A
+//     dependency inside the tile is read from the tile's solution array in
+//     shared memory, spinning while it still holds the sentinel; one in an
+//     earlier tile is read from global memory the same way, with backoff.
+//     There is no barrier between levels: a row waits exactly for its own
+//     dependencies, so the wavefront advances at shared-memory latency.
+//     A row's right-hand side is loaded before its dependencies are awaited.
+// Progress: a record only depends on earlier records, the earliest
+// unfinished record always has its inputs, and the ring always holds it; a
+// tile only depends on earlier tiles, taken by ticket by running CTAs.
+// Every wait is bounded in wall-clock time; on expiry the error word is set,
+// waiters release their dependents with a NaN and the CTA drains its own
+// copies before leaving.
 //
-// OP contract:
+// OP contract (fused vector updates and dot products of the PCG):
 //   void begin();  bool active();  void inactive_end()   (block 0, !active)
-//   T rhs(int row);                 phase A
-//   void done(int row, T y);        phase C
+//   Pre pre(int row)                loads of the rhs (issued early)
+//   T rhs(int row, const Pre&)      rhs value (may store updated vectors)
+//   DPre dpre(int row)              loads for the epilogue
+//   void done(int row, T y, const DPre&)
 //   void chunk_end(tile_ix, ntiles, ticket, sm)   whole block, after the
 //        tile; ticket[1] counts finished tiles (chunk_finished()).
 #pragma once
@@ -42,13 +45,13 @@
 
 namespace gb {
 
-constexpr int kTriConsumers = 4;                       // consumer warps
+constexpr int kTriConsumers = 8;                       // consumer warps
 constexpr int kTriThreads = (kTriConsumers + 1) * 32;  // + one producer warp
 constexpr int kTriSlots = 16;                          // ring depth (records in flight)
 constexpr int kTriSlotBytes = 4096;                    // max record size
 constexpr int kTriRecTable = 1024;                     // records of a tile cached in smem
+constexpr int kTriRecRows = 32;                        // rows per record (one per lane)
 constexpr int kRecLong = 2;                            // record flag: one row, warp-reduced
-constexpr int kRecBarrier = 1;                         // record flag: level ends here
 
 // Record header (16 bytes).  Layout after it, R4 = nrows rounded up to 4:
 //   int rows[R4]; T diag[R4]; T dinv[R4]; int cols[len*R4]; T vals[len*R4]
@@ -65,7 +68,6 @@ struct TriArgs {
   const int* __restrict__ tile_rec;   // [ntiles+1] record range of each tile
   const long long* __restrict__ rec_off;  // [nrec] byte offset in recbuf
   const int* __restrict__ rec_bytes;      // [nrec]
-  const int* __restrict__ rec_flags;      // [nrec] kRecBarrier / kRecLong
   const unsigned char* __restrict__ recbuf;
   const int* __restrict__ long_col;
   const T* __restrict__ long_val;
@@ -108,16 +110,21 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait on an mbarrier phase; false on timeout / abort.
+// Bounded wait on an mbarrier phase; false on timeout / abort.  The clock
+// and the (global) error word are checked only every 64 polls so that a
+// satisfied barrier is noticed at shared-memory speed.
 __device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity, int* err) {
   if (mbar_try_wait(b, parity)) return true;
   const uint64_t t0 = globaltimer_ns();
-  const uint64_t budget = spin_budget(err);
-  while (true) {
+  uint64_t budget = 0;
+  for (unsigned polls = 1;; ++polls) {
     if (mbar_try_wait(b, parity)) return true;
-    if (ld_volatile(err) != 0 || globaltimer_ns() - t0 > budget) {
-      atomicCAS(err, 0, (int)GB_TIMEOUT);
-      return false;
+    if ((polls & 63u) == 0u) {
+      if (!budget) budget = spin_budget(err);
+      if (ld_volatile(err) != 0 || globaltimer_ns() - t0 > budget) {
+        atomicCAS(err, 0, (int)GB_TIMEOUT);
+        return false;
+      }
     }
   }
 }
@@ -128,152 +135,97 @@ __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned
       "l"(src), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
 }
-__device__ __forceinline__ void named_barrier_consumers() {
-  asm volatile("bar.sync 1, %0;" ::"n"(kTriConsumers * 32) : "memory");
-}
 
+// Spin on a tile-local value in shared memory (written by another warp of
+// this CTA).  Bounded like the global waits.
 template <typename T>
-__device__ __forceinline__ T dep_value(const T* y, const T* sm, int c, int t0, int t1, int* err) {
-  if (c >= t0 && c < t1) return sm[c - t0];
-  return wait_value(y + c, err);
-}
-
-// Remote values of a thread's first row in the next record, read before the
-// level barrier so that the dependency chain does not wait on L2.
-constexpr int kTriPrefetchRemote = 2;
-template <typename T>
-struct RemotePrefetch {
-  int col[kTriPrefetchRemote];
-  T val[kTriPrefetchRemote];
-};
-
-template <typename T>
-__device__ __forceinline__ void prefetch_remote(const TriArgs<T>& A, const unsigned char* rec, int t0,
-                                                int t1, int ct, RemotePrefetch<T>& pf) {
-#pragma unroll
-  for (int q = 0; q < kTriPrefetchRemote; ++q) pf.col[q] = -1;
-  const RecHdr h = *reinterpret_cast<const RecHdr*>(rec);
-  if ((h.flags & kRecLong) || ct >= h.nrows) return;
-  const int R4 = (h.nrows + 3) & ~3;
-  const int* cols = reinterpret_cast<const int*>(rec + sizeof(RecHdr) + 4 * R4 + 2 * sizeof(T) * R4);
-  int q = 0;
-  for (int k = 0; k < h.len && q < kTriPrefetchRemote; ++k) {
-    const int c = cols[k * R4 + ct];
-    if (c < 0) break;
-    if (c < t0 || c >= t1) {
-      pf.col[q] = c;
-      pf.val[q] = ld_relaxed(A.y + c);
-      ++q;
+__device__ __forceinline__ T wait_local(const T* p, int* err) {
+  const volatile T* vp = p;
+  T v = *vp;
+  if (!is_sentinel(v)) return v;
+  const uint64_t t0 = globaltimer_ns();
+  uint64_t budget = 0;
+  for (unsigned polls = 1;; ++polls) {
+    v = *vp;
+    if (!is_sentinel(v)) return v;
+    if ((polls & 255u) == 0u) {
+      if (!budget) budget = spin_budget(err);
+      if (ld_volatile(err) != 0 || globaltimer_ns() - t0 > budget) {
+        atomicCAS(err, 0, (int)GB_TIMEOUT);
+        return (T)__int_as_float(0x7FC00000);
+      }
     }
   }
 }
 
-// Solves the rows of one staged record (consumer threads ct = 0..127).
-template <typename T, bool EXACT>
-__device__ __forceinline__ void solve_record(const TriArgs<T>& A, T* sm, int t0, int t1,
-                                             const unsigned char* rec, int ct,
-                                             const RemotePrefetch<T>& pf) {
+template <typename T>
+__device__ __forceinline__ T dep_value(const TriArgs<T>& A, const T* sy, int c, int t0, int t1) {
+  if (c >= t0 && c < t1) return wait_local(sy + (c - t0), A.err);
+  return wait_value(A.y + c, A.err);
+}
+
+__device__ __forceinline__ void st_shared_volatile(double* p, double v) { *(volatile double*)p = v; }
+__device__ __forceinline__ void st_shared_volatile(float* p, float v) { *(volatile float*)p = v; }
+
+// Solves one staged record with one warp (lane = row of the record).
+template <typename T, bool EXACT, typename OP>
+__device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy, int t0, int t1,
+                                             const unsigned char* rec, int lane) {
   const RecHdr h = *reinterpret_cast<const RecHdr*>(rec);
   const int R4 = (h.nrows + 3) & ~3;
   const int* rows = reinterpret_cast<const int*>(rec + sizeof(RecHdr));
   const T* diag = reinterpret_cast<const T*>(rows + R4);
   const T* dinv = diag + R4;
   if (h.flags & kRecLong) {
-    // one row, the whole first consumer warp reduces it
-    if (ct >= 32) return;
+    // one row with many dependencies: the warp splits them
     const int row = rows[0];
+    const typename OP::Pre pr = op.pre(row);
+    const typename OP::DPre dp = op.dpre(row);
     T acc = T(0);
-    for (int k = ct; k < h.len; k += 32) {
+    for (int k = lane; k < h.len; k += 32) {
       const int c = __ldg(A.long_col + h.off + k);
-      acc = fma_rn(__ldg(A.long_val + h.off + k), dep_value(A.y, sm, c, t0, t1, A.err), acc);
+      acc = fma_rn(__ldg(A.long_val + h.off + k), dep_value(A, sy, c, t0, t1), acc);
     }
     acc = warp_sum(acc);
-    if (ct == 0) {
-      const T r = sub_rn(sm[row - t0], acc);
+    if (lane == 0) {
+      const T r = sub_rn(op.rhs(row, pr), acc);
       const T yv = publishable(EXACT ? div_rn(r, diag[0]) : r * dinv[0]);
-      sm[row - t0] = yv;
+      st_shared_volatile(sy + (row - t0), yv);
       st_relaxed(A.y + row, yv);
+      op.done(row, yv, dp);
     }
     return;
   }
+  if (lane >= h.nrows) return;
   const int* cols = reinterpret_cast<const int*>(dinv + R4);
   const T* vals = reinterpret_cast<const T*>(cols + (size_t)h.len * R4);
-  for (int r = ct; r < h.nrows; r += kTriConsumers * 32) {
-    const int row = rows[r];
-    T acc = sm[row - t0];
-    for (int k = 0; k < h.len; ++k) {
-      const int c = cols[k * R4 + r];
-      if (c < 0) break;
-      const T l = vals[k * R4 + r];
-      T v;
-      if (c >= t0 && c < t1) {
-        v = sm[c - t0];
-      } else {
-        v = sentinel<T>();
-        if (r == ct) {
-#pragma unroll
-          for (int q = 0; q < kTriPrefetchRemote; ++q)
-            if (pf.col[q] == c) v = pf.val[q];
-        }
-        if (is_sentinel(v)) v = wait_value(A.y + c, A.err);
-      }
-      acc = EXACT ? sub_rn(acc, mul_rn(l, v)) : fma_rn(-l, v, acc);
-    }
-    const T yv = publishable(EXACT ? div_rn(acc, diag[r]) : acc * dinv[r]);
-    sm[row - t0] = yv;
-    st_relaxed(A.y + row, yv);
+  const int row = rows[lane];
+  const typename OP::Pre pr = op.pre(row);      // independent of the dependencies:
+  const typename OP::DPre dp = op.dpre(row);    // in flight while we wait
+  const T dg = EXACT ? diag[lane] : dinv[lane];
+  T acc = op.rhs(row, pr);
+  for (int k = 0; k < h.len; ++k) {
+    const int c = cols[k * R4 + lane];
+    if (c < 0) break;
+    const T l = vals[k * R4 + lane];
+    const T v = dep_value(A, sy, c, t0, t1);
+    acc = EXACT ? sub_rn(acc, mul_rn(l, v)) : fma_rn(-l, v, acc);
   }
-}
-
-// Phase A / C loops: every thread first issues the loads of kTriUnroll rows
-// (OP::pre / OP::dpre), then computes and stores them, so a tile's vector
-// traffic streams instead of paying one DRAM round trip per row.
-constexpr int kTriUnroll = 8;
-
-template <typename T, typename OP>
-__device__ __forceinline__ void phase_rhs(OP& op, T* sm, int t0, int t1) {
-  for (int b = t0 + (int)threadIdx.x; b < t1; b += kTriUnroll * kTriThreads) {
-    typename OP::Pre pr[kTriUnroll];
-#pragma unroll
-    for (int u = 0; u < kTriUnroll; ++u) {
-      const int i = b + u * kTriThreads;
-      if (i < t1) pr[u] = op.pre(i);
-    }
-#pragma unroll
-    for (int u = 0; u < kTriUnroll; ++u) {
-      const int i = b + u * kTriThreads;
-      if (i < t1) sm[i - t0] = op.rhs(i, pr[u]);
-    }
-  }
-}
-
-template <typename T, typename OP>
-__device__ __forceinline__ void phase_done(OP& op, const T* sm, int t0, int t1) {
-  for (int b = t0 + (int)threadIdx.x; b < t1; b += kTriUnroll * kTriThreads) {
-    typename OP::DPre pr[kTriUnroll];
-#pragma unroll
-    for (int u = 0; u < kTriUnroll; ++u) {
-      const int i = b + u * kTriThreads;
-      if (i < t1) pr[u] = op.dpre(i);
-    }
-#pragma unroll
-    for (int u = 0; u < kTriUnroll; ++u) {
-      const int i = b + u * kTriThreads;
-      if (i < t1) op.done(i, sm[i - t0], pr[u]);
-    }
-  }
+  const T yv = publishable(EXACT ? div_rn(acc, dg) : acc * dg);
+  st_shared_volatile(sy + (row - t0), yv);
+  st_relaxed(A.y + row, yv);
+  op.done(row, yv, dp);
 }
 
 template <typename T, typename OP, bool EXACT>
 __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP op) {
   extern __shared__ __align__(128) unsigned char tri_smem[];
-  unsigned char* ring = tri_smem;                                   // kTriSlots x kTriSlotBytes
-  T* sm = reinterpret_cast<T*>(tri_smem + kTriSlots * kTriSlotBytes);  // tile values
+  unsigned char* ring = tri_smem;                                     // kTriSlots x kTriSlotBytes
+  T* sy = reinterpret_cast<T*>(tri_smem + kTriSlots * kTriSlotBytes);  // tile solution
   __shared__ __align__(8) uint64_t full_bar[kTriSlots], empty_bar[kTriSlots];
   __shared__ long long s_roff[kTriRecTable];
   __shared__ int s_rbytes[kTriRecTable];
-  __shared__ int s_rflags[kTriRecTable];
-  __shared__ unsigned s_issued, s_consumed;
+  __shared__ unsigned s_issued;
   __shared__ int s_tile;
   __shared__ double s_red[64];
   op.begin();
@@ -281,18 +233,18 @@ __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP 
     if (blockIdx.x == 0 && threadIdx.x == 0) op.inactive_end();
     return;  // no ticket touched
   }
-  const int wid = threadIdx.x >> 5;
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool producer = wid == kTriConsumers;
   if (threadIdx.x == 0) {
     for (int s = 0; s < kTriSlots; ++s) {
       mbar_init(&full_bar[s], 1);
-      mbar_init(&empty_bar[s], kTriConsumers);
+      mbar_init(&empty_bar[s], 1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  unsigned issued = 0;    // records issued by this CTA's producer (all tiles)
-  unsigned consumed = 0;  // records consumed by this CTA's consumers
+  unsigned base = 0;       // records of earlier tiles streamed by this CTA
+  unsigned issued = 0;     // producer: records issued (all tiles)
   bool failed = false;
   while (true) {
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(&A.ticket[0], 1u);
@@ -302,84 +254,63 @@ __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP 
     if (k >= A.ntiles) break;
     const int t0 = __ldg(A.tile_row0 + k), t1 = __ldg(A.tile_row1 + k);
     const int rec0 = __ldg(A.tile_rec + k), rec1 = __ldg(A.tile_rec + k + 1);
-    // the tile's record table, so the producer issues copies back to back
-    for (int q = threadIdx.x; q < rec1 - rec0 && q < kTriRecTable; q += kTriThreads) {
+    const int nrec = rec1 - rec0;
+    for (int q = threadIdx.x; q < nrec && q < kTriRecTable; q += kTriThreads) {
       s_roff[q] = __ldg(A.rec_off + rec0 + q);
       s_rbytes[q] = __ldg(A.rec_bytes + rec0 + q);
-      s_rflags[q] = __ldg(A.rec_flags + rec0 + q);
     }
-    // A) right-hand sides
-    phase_rhs<T>(op, sm, t0, t1);
+    for (int i = threadIdx.x; i < t1 - t0; i += kTriThreads) sy[i] = sentinel<T>();
     __syncthreads();
-    // B) records
     if (producer) {
-      if ((threadIdx.x & 31) == 0) {
-        for (int j = rec0; j < rec1 && !failed; ++j, ++issued) {
-          const int slot = issued % kTriSlots;
-          const unsigned use = issued / kTriSlots;
-          if (!mbar_wait(&empty_bar[slot], (use & 1u) ^ 1u, A.err)) {
+      if (lane == 0) {
+        for (int q = 0; q < nrec && !failed; ++q, ++issued) {
+          const unsigned u = base + q;
+          const int slot = u % kTriSlots;
+          if ((q & 15) == 15 && ld_volatile(A.err) != 0) {
             failed = true;
             break;
           }
-          const int q = j - rec0;
-          const unsigned bytes = (unsigned)(q < kTriRecTable ? s_rbytes[q] : __ldg(A.rec_bytes + j));
-          const long long off = q < kTriRecTable ? s_roff[q] : __ldg(A.rec_off + j);
+          if (!mbar_wait(&empty_bar[slot], ((u / kTriSlots) & 1u) ^ 1u, A.err)) {
+            failed = true;
+            break;
+          }
+          const unsigned bytes = (unsigned)(q < kTriRecTable ? s_rbytes[q] : __ldg(A.rec_bytes + rec0 + q));
+          const long long off = q < kTriRecTable ? s_roff[q] : __ldg(A.rec_off + rec0 + q);
           mbar_expect_tx(&full_bar[slot], bytes);
           tma_load_1d(ring + slot * kTriSlotBytes, A.recbuf + off, bytes, &full_bar[slot]);
         }
       }
-      issued = __shfl_sync(0xffffffffu, issued, 0);
-      failed = __shfl_sync(0xffffffffu, failed, 0);
+      __syncwarp();
     } else {
-      const int ct = threadIdx.x;
-      RemotePrefetch<T> pf;
-#pragma unroll
-      for (int q = 0; q < kTriPrefetchRemote; ++q) pf.col[q] = -1;
-      for (int j = rec0; j < rec1; ++j, ++consumed) {
-        const int slot = consumed % kTriSlots;
-        const unsigned use = consumed / kTriSlots;
-        if (!failed && !mbar_wait(&full_bar[slot], use & 1u, A.err)) failed = true;
-        const unsigned char* rec = ring + slot * kTriSlotBytes;
-        if (!failed) {
-          solve_record<T, EXACT>(A, sm, t0, t1, rec, ct, pf);
-        }
+      for (int q = wid; q < nrec; q += kTriConsumers) {
+        const unsigned u = base + q;
+        const int slot = u % kTriSlots;
+        if (!failed && !mbar_wait(&full_bar[slot], (u / kTriSlots) & 1u, A.err)) failed = true;
+        if (!failed) solve_record<T, EXACT>(A, op, sy, t0, t1, ring + slot * kTriSlotBytes, lane);
         __syncwarp();
-        if ((ct & 31) == 0) mbar_arrive(&empty_bar[slot]);
-        // if the next record is staged already, read its remote values now,
-        // before the level barrier (never wait for it here)
-#pragma unroll
-        for (int q = 0; q < kTriPrefetchRemote; ++q) pf.col[q] = -1;
-        if (!failed && j + 1 < rec1) {
-          const unsigned nx = consumed + 1;
-          if (mbar_try_wait(&full_bar[nx % kTriSlots], (nx / kTriSlots) & 1u))
-            prefetch_remote(A, ring + (nx % kTriSlots) * kTriSlotBytes, t0, t1, ct, pf);
-        }
-        // level ends: every consumer warp reads the same table, so all take
-        // the same barriers even if one of them gave up waiting for a record
-        const int q = j - rec0;
-        const int fl = q < kTriRecTable ? s_rflags[q] : __ldg(A.rec_flags + j);
-        if (fl & kRecBarrier) named_barrier_consumers();
+        // after a failure the slot is not released: its copy may still be in
+        // flight, and the producer must not aim another copy at it
+        if (lane == 0 && !failed) mbar_arrive(&empty_bar[slot]);
       }
     }
+    base += nrec;
     __syncthreads();
-    // C) epilogue
-    phase_done<T>(op, sm, t0, t1);
     op.chunk_end(k, A.ntiles, A.ticket, s_red);
     __syncthreads();
   }
-  // Drain: every issued copy has been consumed (consumers wait on each full
-  // barrier, or fail only after the error word is set; in that case wait,
-  // bounded, for the copies still in flight before the CTA's shared memory
-  // goes away).
-  if (threadIdx.x == 0) s_consumed = consumed;
+  // Drain: every issued copy must have landed before the CTA's shared
+  // memory goes away.  A slot is reused only after its previous record was
+  // consumed, so only the last ring window of issues can still be in
+  // flight (after a timeout); wait for those, bounded.
   if (threadIdx.x == kTriConsumers * 32) s_issued = issued;
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (unsigned u = s_consumed; u < s_issued; ++u) {
+    const unsigned last = s_issued;
+    for (unsigned u = last > (unsigned)kTriSlots ? last - kTriSlots : 0u; u < last; ++u) {
       const int slot = u % kTriSlots;
-      const uint64_t t0 = globaltimer_ns();
+      const uint64_t w0 = globaltimer_ns();
       while (!mbar_try_wait(&full_bar[slot], (u / kTriSlots) & 1u) &&
-             globaltimer_ns() - t0 < kSpinBudgetNs) {
+             globaltimer_ns() - w0 < kSpinBudgetNs) {
       }
     }
   }

@@ -75,7 +75,7 @@ void layout(const TriDeps& d, const std::vector<RecDesc>& recs, int S, std::vect
     int* hdr = reinterpret_cast<int*>(buf.data() + base);
     hdr[0] = nrows;
     hdr[1] = r.len;
-    hdr[2] = (r.tile_level_end ? kRecBarrier : 0) | (r.is_long ? kRecLong : 0);
+    hdr[2] = r.is_long ? kRecLong : 0;
     hdr[3] = 0;
     int* rows = hdr + 4;
     for (long long t = 0; t < R4; ++t) rows[t] = t < nrows ? r.rows[t] : -1;
@@ -213,17 +213,18 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
         r.is_long = false;
         r.len = deps_of(rows[p]);
         r.rows.push_back(rows[p++]);  // a SHORT row (<= kLongDeps deps) always fits a slot
-        while (p < rows.size() && rec_size((int)r.rows.size() + 1, r.len, 8) <= kTriSlotBytes) {
+        while (p < rows.size() && (int)r.rows.size() < kTriRecRows &&
+               rec_size((int)r.rows.size() + 1, r.len, 8) <= kTriSlotBytes) {
           r.rows.push_back(rows[p]);
           ++p;
         }
         recs.push_back(r);
       }
-      if (recs.size() > first_rec) recs.back().tile_level_end = 1;
+      (void)first_rec;
     }
     tile_rec.push_back((int)recs.size());
   }
-  for (const RecDesc& r : recs) rec_flags.push_back((r.tile_level_end ? kRecBarrier : 0) | (r.is_long ? kRecLong : 0));
+  for (const RecDesc& r : recs) rec_flags.push_back(r.is_long ? kRecLong : 0);
 
   std::vector<unsigned char> buf;
   std::vector<long long> off, vdst, ddst, idst;
@@ -339,7 +340,6 @@ TriArgs<T> tri_args(const TriPlan& p, T* y, int* err) {
   A.tile_rec = p.tile_rec;
   A.rec_off = rs.off;
   A.rec_bytes = rs.nbytes;
-  A.rec_flags = p.rec_flags;
   A.recbuf = rs.buf;
   A.long_col = p.long_col;
   A.long_val = (const T*)rs.long_val;
