@@ -47,8 +47,9 @@ namespace gb {
 
 constexpr int kTriConsumers = 8;                       // consumer warps
 constexpr int kTriThreads = (kTriConsumers + 1) * 32;  // + one producer warp
-constexpr int kTriSlots = 16;                          // ring depth (records in flight)
-constexpr int kTriSlotBytes = 4096;                    // max record size
+constexpr int kTriSlots = 40;                          // ring depth (records in flight)
+constexpr int kTriSlotBytes = 2048;                    // max record size
+constexpr int kTriL2Ahead = 32;                        // records prefetched into L2 ahead of the ring
 constexpr int kTriRecTable = 1024;                     // records of a tile cached in smem
 constexpr int kTriRecRows = 32;                        // rows per record (one per lane)
 constexpr int kRecLong = 2;                            // record flag: one row, warp-reduced
@@ -128,6 +129,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity, int* err
     }
   }
 }
+__device__ __forceinline__ void tma_prefetch_l2(const void* src, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
   asm volatile(
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
@@ -203,12 +207,30 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
   const typename OP::Pre pr = op.pre(row);      // independent of the dependencies:
   const typename OP::DPre dp = op.dpre(row);    // in flight while we wait
   const T dg = EXACT ? diag[lane] : dinv[lane];
+  // issue the first remote (other-tile) reads now; they are usually ready
+  // by the time the local dependencies are
+  constexpr int kEarly = 4;
+  T early[kEarly];
+#pragma unroll
+  for (int k = 0; k < kEarly; ++k) {
+    early[k] = sentinel<T>();
+    if (k < h.len) {
+      const int c = cols[k * R4 + lane];
+      if (c >= 0 && (c < t0 || c >= t1)) early[k] = ld_relaxed(A.y + c);
+    }
+  }
   T acc = op.rhs(row, pr);
   for (int k = 0; k < h.len; ++k) {
     const int c = cols[k * R4 + lane];
     if (c < 0) break;
     const T l = vals[k * R4 + lane];
-    const T v = dep_value(A, sy, c, t0, t1);
+    T v;
+    if (c >= t0 && c < t1) {
+      v = wait_local(sy + (c - t0), A.err);
+    } else {
+      v = k < kEarly ? early[k] : sentinel<T>();
+      if (is_sentinel(v)) v = wait_value(A.y + c, A.err);
+    }
     acc = EXACT ? sub_rn(acc, mul_rn(l, v)) : fma_rn(-l, v, acc);
   }
   const T yv = publishable(EXACT ? div_rn(acc, dg) : acc * dg);
@@ -278,6 +300,9 @@ __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP 
           const long long off = q < kTriRecTable ? s_roff[q] : __ldg(A.rec_off + rec0 + q);
           mbar_expect_tx(&full_bar[slot], bytes);
           tma_load_1d(ring + slot * kTriSlotBytes, A.recbuf + off, bytes, &full_bar[slot]);
+          // warm L2 with a record further ahead, so ring copies hit L2
+          const int qa = q + kTriL2Ahead;
+          if (qa < nrec && qa < kTriRecTable) tma_prefetch_l2(A.recbuf + s_roff[qa], (unsigned)s_rbytes[qa]);
         }
       }
       __syncwarp();
@@ -338,7 +363,7 @@ int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   static bool attr_set = false;  // one per instantiation
   if (!attr_set) {
     GB_CUDA_TRY(cudaFuncSetAttribute(tri_tile_kernel<T, OP, EXACT>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 212 * 1024));
     attr_set = true;
   }
   int per_sm = 0;

@@ -35,7 +35,11 @@ int tri_default_tile_rows(int n) {
 
 namespace {
 
-constexpr int kLongDeps = 64;  // rows with more dependencies get a LONG record
+// Rows with more dependencies get a LONG record.  A SHORT record holding a
+// single row of kLongDeps dependencies must fit a ring slot:
+// 16 + 4*4 + 2*8*4 + kLongDeps*4*12 <= kTriSlotBytes.
+constexpr int kLongDeps = 32;
+static_assert(16 + 16 + 64 + kLongDeps * 4 * 12 <= kTriSlotBytes, "record slot too small");
 
 inline long long align16(long long b) { return (b + 15) & ~15LL; }
 
@@ -230,6 +234,8 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
   std::vector<long long> off, vdst, ddst, idst;
   std::vector<int> nbytes, vsrc, dsrc, long_col, long_src;
   layout(d, recs, 8, buf, off, nbytes, vdst, ddst, idst, &vsrc, &dsrc, &long_col, &long_src);
+  for (int b : nbytes)  // every staged copy must fit its slot
+    if (b <= 0 || b > kTriSlotBytes || (b & 15)) return GB_BAD_INPUT;
   plan->nval = (int)vsrc.size();
   plan->ndiag = (int)dsrc.size();
   plan->nlong = (int)long_col.size();
