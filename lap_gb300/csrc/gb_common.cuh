@@ -95,12 +95,39 @@ __device__ __forceinline__ uint64_t spin_budget(const int* err) {
 // rows at the front.
 constexpr unsigned kMaxSleepNs = 256u;
 
+// Timeout bookkeeping shared by the spin loops.  Only the clock (a special
+// register) is read while spinning; the error word in global memory -- set
+// when another waiter gave up -- is consulted only once a wait has lasted
+// kErrCheckAfterNs, so a satisfied dependency is never noticed late because
+// of a slow global load.
+constexpr uint64_t kErrCheckAfterNs = 1000000ull;  // 1 ms
+
+struct SpinClock {
+  uint64_t t0 = 0;
+  uint64_t budget = 0;
+  // true: give up (timeout recorded in *err)
+  __device__ __forceinline__ bool expired(int* err) {
+    const uint64_t now = globaltimer_ns();
+    if (t0 == 0) {
+      t0 = now;
+      return false;
+    }
+    const uint64_t waited = now - t0;
+    if (!budget) budget = spin_budget(err);  // one global read per long wait
+    if (waited < kErrCheckAfterNs && waited <= budget) return false;
+    if (ld_volatile(err) != 0 || waited > budget) {
+      atomicCAS(err, 0, (int)GB_TIMEOUT);
+      return true;
+    }
+    return false;
+  }
+};
+
 template <typename T>
 __device__ __forceinline__ T wait_value(const T* p, int* err) {
   T v = ld_relaxed(p);
   if (!is_sentinel(v)) return v;
-  const uint64_t t0 = globaltimer_ns();
-  const uint64_t budget = spin_budget(err);
+  SpinClock clk;
   unsigned polls = 0, ns = 32u;
   while (true) {
     // the first polls spin (a value on the critical path usually lands
@@ -111,12 +138,7 @@ __device__ __forceinline__ T wait_value(const T* p, int* err) {
     }
     v = ld_relaxed(p);
     if (!is_sentinel(v)) return v;
-    if ((++polls & kPollCheck) == 0u) {
-      if (ld_volatile(err) != 0 || globaltimer_ns() - t0 > budget) {
-        atomicCAS(err, 0, (int)GB_TIMEOUT);
-        return (T)__int_as_float(0x7FC00000);
-      }
-    }
+    if ((++polls & kPollCheck) == 0u && clk.expired(err)) return (T)__int_as_float(0x7FC00000);
   }
 }
 
@@ -131,6 +153,7 @@ __device__ __forceinline__ bool wait_flag(const int* flag, int* err) {
     if (ns < kMaxSleepNs) ns <<= 1;
     if (ld_acquire(flag) != 0) return true;
     if ((++polls & kPollCheck) == 0u) {
+      // setup-time wait (IC(0) factorization): the simple check is fine
       if (ld_volatile(err) != 0 || globaltimer_ns() - t0 > budget) {
         atomicCAS(err, 0, (int)GB_TIMEOUT);
         return false;

@@ -116,17 +116,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
 // satisfied barrier is noticed at shared-memory speed.
 __device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity, int* err) {
   if (mbar_try_wait(b, parity)) return true;
-  const uint64_t t0 = globaltimer_ns();
-  uint64_t budget = 0;
+  SpinClock clk;
   for (unsigned polls = 1;; ++polls) {
     if (mbar_try_wait(b, parity)) return true;
-    if ((polls & 63u) == 0u) {
-      if (!budget) budget = spin_budget(err);
-      if (ld_volatile(err) != 0 || globaltimer_ns() - t0 > budget) {
-        atomicCAS(err, 0, (int)GB_TIMEOUT);
-        return false;
-      }
-    }
+    if ((polls & 63u) == 0u && clk.expired(err)) return false;
   }
 }
 __device__ __forceinline__ void tma_prefetch_l2(const void* src, unsigned bytes) {
@@ -147,18 +140,11 @@ __device__ __forceinline__ T wait_local(const T* p, int* err) {
   const volatile T* vp = p;
   T v = *vp;
   if (!is_sentinel(v)) return v;
-  const uint64_t t0 = globaltimer_ns();
-  uint64_t budget = 0;
+  SpinClock clk;
   for (unsigned polls = 1;; ++polls) {
     v = *vp;
     if (!is_sentinel(v)) return v;
-    if ((polls & 255u) == 0u) {
-      if (!budget) budget = spin_budget(err);
-      if (ld_volatile(err) != 0 || globaltimer_ns() - t0 > budget) {
-        atomicCAS(err, 0, (int)GB_TIMEOUT);
-        return (T)__int_as_float(0x7FC00000);
-      }
-    }
+    if ((polls & 255u) == 0u && clk.expired(err)) return (T)__int_as_float(0x7FC00000);
   }
 }
 
