@@ -205,18 +205,38 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
       if (c >= 0 && (c < t0 || c >= t1)) early[k] = ld_relaxed(A.y + c);
     }
   }
+  // wait for the first kHeld dependency values before touching the rhs, so
+  // the rhs loads stay in flight while the row waits for its inputs
+  constexpr int kHeld = 8;
+  T held[kHeld];
+  const int nh = h.len < kHeld ? h.len : kHeld;
+#pragma unroll
+  for (int k = 0; k < kHeld; ++k) {
+    held[k] = T(0);
+    if (k < nh) {
+      const int c = cols[k * R4 + lane];
+      if (c >= t0 && c < t1) {
+        held[k] = wait_local(sy + (c - t0), A.err);
+      } else if (c >= 0) {
+        T v = k < kEarly ? early[k] : sentinel<T>();
+        held[k] = is_sentinel(v) ? wait_value(A.y + c, A.err) : v;
+      }
+    }
+  }
+  // the reference's order: acc = rhs; acc -= l_k * y_k for k ascending
   T acc = op.rhs(row, pr);
-  for (int k = 0; k < h.len; ++k) {
+#pragma unroll
+  for (int k = 0; k < kHeld; ++k) {
+    if (k < nh && cols[k * R4 + lane] >= 0) {
+      const T l = vals[k * R4 + lane];
+      acc = EXACT ? sub_rn(acc, mul_rn(l, held[k])) : fma_rn(-l, held[k], acc);
+    }
+  }
+  for (int k = kHeld; k < h.len; ++k) {
     const int c = cols[k * R4 + lane];
     if (c < 0) break;
     const T l = vals[k * R4 + lane];
-    T v;
-    if (c >= t0 && c < t1) {
-      v = wait_local(sy + (c - t0), A.err);
-    } else {
-      v = k < kEarly ? early[k] : sentinel<T>();
-      if (is_sentinel(v)) v = wait_value(A.y + c, A.err);
-    }
+    const T v = (c >= t0 && c < t1) ? wait_local(sy + (c - t0), A.err) : wait_value(A.y + c, A.err);
     acc = EXACT ? sub_rn(acc, mul_rn(l, v)) : fma_rn(-l, v, acc);
   }
   const T yv = publishable(EXACT ? div_rn(acc, dg) : acc * dg);
