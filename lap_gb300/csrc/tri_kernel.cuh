@@ -134,24 +134,34 @@ __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned
 }
 
 // Spin on a tile-local value in shared memory (written by another warp of
-// this CTA).  Bounded like the global waits.
+// this CTA).  Bounded like the global waits.  The spin loops are kept out of
+// line so that the unrolled row code stays small; only the first read is
+// inlined.
 template <typename T>
-__device__ __forceinline__ T wait_local(const T* p, int* err) {
+__device__ __noinline__ T wait_local_slow(const T* p, int* err) {
   const volatile T* vp = p;
-  T v = *vp;
-  if (!is_sentinel(v)) return v;
   SpinClock clk;
   for (unsigned polls = 1;; ++polls) {
-    v = *vp;
+    const T v = *vp;
     if (!is_sentinel(v)) return v;
     if ((polls & 255u) == 0u && clk.expired(err)) return (T)__int_as_float(0x7FC00000);
   }
+}
+template <typename T>
+__device__ __forceinline__ T wait_local(const T* p, int* err) {
+  const T v = *(const volatile T*)p;
+  return is_sentinel(v) ? wait_local_slow(p, err) : v;
+}
+template <typename T>
+__device__ __noinline__ T wait_value_slow(const T* p, int* err) {
+  return wait_value(p, err);
 }
 
 template <typename T>
 __device__ __forceinline__ T dep_value(const TriArgs<T>& A, const T* sy, int c, int t0, int t1) {
   if (c >= t0 && c < t1) return wait_local(sy + (c - t0), A.err);
-  return wait_value(A.y + c, A.err);
+  const T v = ld_relaxed(A.y + c);
+  return is_sentinel(v) ? wait_value_slow(A.y + c, A.err) : v;
 }
 
 __device__ __forceinline__ void st_shared_volatile(double* p, double v) { *(volatile double*)p = v; }
@@ -207,7 +217,7 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
   }
   // wait for the first kHeld dependency values before touching the rhs, so
   // the rhs loads stay in flight while the row waits for its inputs
-  constexpr int kHeld = 8;
+  constexpr int kHeld = kEarly;
   T held[kHeld];
   const int nh = h.len < kHeld ? h.len : kHeld;
 #pragma unroll
@@ -218,8 +228,7 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
       if (c >= t0 && c < t1) {
         held[k] = wait_local(sy + (c - t0), A.err);
       } else if (c >= 0) {
-        T v = k < kEarly ? early[k] : sentinel<T>();
-        held[k] = is_sentinel(v) ? wait_value(A.y + c, A.err) : v;
+        held[k] = is_sentinel(early[k]) ? wait_value_slow(A.y + c, A.err) : early[k];
       }
     }
   }
@@ -236,7 +245,7 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
     const int c = cols[k * R4 + lane];
     if (c < 0) break;
     const T l = vals[k * R4 + lane];
-    const T v = (c >= t0 && c < t1) ? wait_local(sy + (c - t0), A.err) : wait_value(A.y + c, A.err);
+    const T v = (c >= t0 && c < t1) ? wait_local(sy + (c - t0), A.err) : wait_value_slow(A.y + c, A.err);
     acc = EXACT ? sub_rn(acc, mul_rn(l, v)) : fma_rn(-l, v, acc);
   }
   const T yv = publishable(EXACT ? div_rn(acc, dg) : acc * dg);
