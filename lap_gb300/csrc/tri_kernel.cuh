@@ -54,12 +54,16 @@ constexpr int kTriRecTable = 1024;                     // records of a tile cach
 constexpr int kTriRecRows = 32;                        // rows per record (one per lane)
 constexpr int kRecLong = 2;                            // record flag: one row, warp-reduced
 
-// Record header (16 bytes).  Layout after it, R4 = nrows rounded up to 4:
+// Record header (32 bytes).  Layout after it, R4 = nrows rounded up to 4:
 //   int rows[R4]; T diag[R4]; T dinv[R4]; int cols[len*R4]; T vals[len*R4]
 // (LONG records: no cols/vals; they live at long_col/long_val[off ...]).
+// wait_for = number of the tile's records in earlier tile-levels: the record
+// may start once that many records of the tile are complete.
 struct RecHdr {
-  int nrows, len, flags, off;
+  int nrows, len, flags, off, wait_for, pad0, pad1, pad2;
 };
+constexpr int kRecHdrBytes = (int)sizeof(RecHdr);
+static_assert(kRecHdrBytes == 32, "record header layout");
 
 template <typename T>
 struct TriArgs {
@@ -167,95 +171,105 @@ __device__ __forceinline__ T dep_value(const TriArgs<T>& A, const T* sy, int c, 
 __device__ __forceinline__ void st_shared_volatile(double* p, double v) { *(volatile double*)p = v; }
 __device__ __forceinline__ void st_shared_volatile(float* p, float v) { *(volatile float*)p = v; }
 
-// Solves one staged record with one warp (lane = row of the record).
+// Waits (warp-uniform, lane 0 polls) until `need` records of the current
+// tile are complete, i.e. every earlier tile-level of this record is done.
+static __device__ __noinline__ void wait_level_slow(const int* s_done, int need, int* err) {
+  SpinClock clk;
+  for (unsigned polls = 1;; ++polls) {
+    if (*(const volatile int*)s_done >= need) return;
+    if ((polls & 255u) == 0u && clk.expired(err)) return;
+  }
+}
+__device__ __forceinline__ void wait_level(const int* s_done, int need, int* err, int lane) {
+  if (need <= 0) return;
+  if (lane == 0 && *(const volatile int*)s_done < need) wait_level_slow(s_done, need, err);
+  __syncwarp();
+  __threadfence_block();
+}
+
+// Solves one staged record with one warp (lane = row of the record; a LONG
+// record's single row is split across the warp).  The rhs is formed first
+// (its loads and FP64 updates are independent of the dependencies), then the
+// warp waits for the record's earlier tile-levels, reads tile-local values
+// from shared memory and other tiles' values from global memory (read early,
+// re-read with backoff only if not yet produced), and finally counts itself
+// complete.
 template <typename T, bool EXACT, typename OP>
 __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy, int t0, int t1,
-                                             const unsigned char* rec, int lane) {
+                                             const unsigned char* rec, int lane, int* s_done) {
   const RecHdr h = *reinterpret_cast<const RecHdr*>(rec);
   const int R4 = (h.nrows + 3) & ~3;
   const int* rows = reinterpret_cast<const int*>(rec + sizeof(RecHdr));
   const T* diag = reinterpret_cast<const T*>(rows + R4);
   const T* dinv = diag + R4;
-  if (h.flags & kRecLong) {
-    // one row with many dependencies: the warp splits them
-    const int row = rows[0];
-    const typename OP::Pre pr = op.pre(row);
-    const typename OP::DPre dp = op.dpre(row);
-    T acc = T(0);
-    for (int k = lane; k < h.len; k += 32) {
-      const int c = __ldg(A.long_col + h.off + k);
-      acc = fma_rn(__ldg(A.long_val + h.off + k), dep_value(A, sy, c, t0, t1), acc);
-    }
-    acc = warp_sum(acc);
-    if (lane == 0) {
-      const T r = sub_rn(op.rhs(row, pr), acc);
-      const T yv = publishable(EXACT ? div_rn(r, diag[0]) : r * dinv[0]);
-      st_shared_volatile(sy + (row - t0), yv);
-      st_relaxed(A.y + row, yv);
-      op.done(row, yv, dp);
-    }
-    return;
+  const bool lng = (h.flags & kRecLong) != 0;
+  const bool act = lng ? true : lane < h.nrows;
+  const int row = act ? rows[lng ? 0 : lane] : -1;
+  typename OP::Pre pr;
+  typename OP::DPre dp;
+  if (act) {
+    pr = op.pre(row);
+    dp = op.dpre(row);
   }
-  if (lane >= h.nrows) return;
   const int* cols = reinterpret_cast<const int*>(dinv + R4);
   const T* vals = reinterpret_cast<const T*>(cols + (size_t)h.len * R4);
-  const int row = rows[lane];
-  const typename OP::Pre pr = op.pre(row);      // independent of the dependencies:
-  const typename OP::DPre dp = op.dpre(row);    // in flight while we wait
-  const T dg = EXACT ? diag[lane] : dinv[lane];
-  // issue the first remote (other-tile) reads now; they are usually ready
-  // by the time the local dependencies are
   constexpr int kEarly = 4;
   T early[kEarly];
 #pragma unroll
   for (int k = 0; k < kEarly; ++k) {
     early[k] = sentinel<T>();
-    if (k < h.len) {
+    if (!lng && act && k < h.len) {
       const int c = cols[k * R4 + lane];
       if (c >= 0 && (c < t0 || c >= t1)) early[k] = ld_relaxed(A.y + c);
     }
   }
-  // wait for the first kHeld dependency values before touching the rhs, so
-  // the rhs loads stay in flight while the row waits for its inputs
-  constexpr int kHeld = kEarly;
-  T held[kHeld];
-  const int nh = h.len < kHeld ? h.len : kHeld;
-#pragma unroll
-  for (int k = 0; k < kHeld; ++k) {
-    held[k] = T(0);
-    if (k < nh) {
+  T acc = T(0);
+  if (act && (!lng || lane == 0)) acc = op.rhs(row, pr);
+  wait_level(s_done, h.wait_for, A.err, lane);
+  if (lng) {
+    T s = T(0);
+    for (int k = lane; k < h.len; k += 32) {
+      const int c = __ldg(A.long_col + h.off + k);
+      const T v = (c >= t0 && c < t1) ? sy[c - t0] : dep_value(A, sy, c, t0, t1);
+      s = fma_rn(__ldg(A.long_val + h.off + k), v, s);
+    }
+    s = warp_sum(s);
+    if (lane == 0) {
+      const T r = sub_rn(acc, s);
+      const T yv = publishable(EXACT ? div_rn(r, diag[0]) : r * dinv[0]);
+      sy[row - t0] = yv;
+      st_relaxed(A.y + row, yv);
+      op.done(row, yv, dp);
+    }
+  } else if (act) {
+    // the reference's order: acc = rhs; acc -= l_k * y_k for k ascending
+    for (int k = 0; k < h.len; ++k) {
       const int c = cols[k * R4 + lane];
-      if (c >= t0 && c < t1) {
-        held[k] = wait_local(sy + (c - t0), A.err);
-      } else if (c >= 0) {
-        held[k] = is_sentinel(early[k]) ? wait_value_slow(A.y + c, A.err) : early[k];
-      }
-    }
-  }
-  // the reference's order: acc = rhs; acc -= l_k * y_k for k ascending
-  T acc = op.rhs(row, pr);
-#pragma unroll
-  for (int k = 0; k < kHeld; ++k) {
-    if (k < nh && cols[k * R4 + lane] >= 0) {
+      if (c < 0) break;
       const T l = vals[k * R4 + lane];
-      acc = EXACT ? sub_rn(acc, mul_rn(l, held[k])) : fma_rn(-l, held[k], acc);
+      T v;
+      if (c >= t0 && c < t1) {
+        v = sy[c - t0];  // an earlier tile-level: complete
+      } else {
+        v = k < kEarly ? early[k] : sentinel<T>();
+        if (is_sentinel(v)) v = wait_value_slow(A.y + c, A.err);
+      }
+      acc = EXACT ? sub_rn(acc, mul_rn(l, v)) : fma_rn(-l, v, acc);
     }
+    const T yv = publishable(EXACT ? div_rn(acc, diag[lane]) : acc * dinv[lane]);
+    sy[row - t0] = yv;
+    st_relaxed(A.y + row, yv);
+    op.done(row, yv, dp);
   }
-  for (int k = kHeld; k < h.len; ++k) {
-    const int c = cols[k * R4 + lane];
-    if (c < 0) break;
-    const T l = vals[k * R4 + lane];
-    const T v = (c >= t0 && c < t1) ? wait_local(sy + (c - t0), A.err) : wait_value_slow(A.y + c, A.err);
-    acc = EXACT ? sub_rn(acc, mul_rn(l, v)) : fma_rn(-l, v, acc);
+  __syncwarp();
+  if (lane == 0) {
+    __threadfence_block();
+    atomicAdd(s_done, 1);
   }
-  const T yv = publishable(EXACT ? div_rn(acc, dg) : acc * dg);
-  st_shared_volatile(sy + (row - t0), yv);
-  st_relaxed(A.y + row, yv);
-  op.done(row, yv, dp);
 }
 
 template <typename T, typename OP, bool EXACT>
-__global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP op) {
+__global__ void __launch_bounds__(kTriThreads, 1) tri_tile_kernel(TriArgs<T> A, OP op) {
   extern __shared__ __align__(128) unsigned char tri_smem[];
   unsigned char* ring = tri_smem;                                     // kTriSlots x kTriSlotBytes
   T* sy = reinterpret_cast<T*>(tri_smem + kTriSlots * kTriSlotBytes);  // tile solution
@@ -264,6 +278,7 @@ __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP 
   __shared__ int s_rbytes[kTriRecTable];
   __shared__ unsigned s_issued;
   __shared__ int s_tile;
+  __shared__ int s_done;  // records of the current tile completed
   __shared__ double s_red[64];
   op.begin();
   if (!op.active()) {
@@ -297,6 +312,7 @@ __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP 
       s_rbytes[q] = __ldg(A.rec_bytes + rec0 + q);
     }
     for (int i = threadIdx.x; i < t1 - t0; i += kTriThreads) sy[i] = sentinel<T>();
+    if (threadIdx.x == 0) s_done = 0;
     __syncthreads();
     if (producer) {
       if (lane == 0) {
@@ -326,7 +342,7 @@ __global__ void __launch_bounds__(kTriThreads) tri_tile_kernel(TriArgs<T> A, OP 
         const unsigned u = base + q;
         const int slot = u % kTriSlots;
         if (!failed && !mbar_wait(&full_bar[slot], (u / kTriSlots) & 1u, A.err)) failed = true;
-        if (!failed) solve_record<T, EXACT>(A, op, sy, t0, t1, ring + slot * kTriSlotBytes, lane);
+        if (!failed) solve_record<T, EXACT>(A, op, sy, t0, t1, ring + slot * kTriSlotBytes, lane, &s_done);
         __syncwarp();
         // after a failure the slot is not released: its copy may still be in
         // flight, and the producer must not aim another copy at it

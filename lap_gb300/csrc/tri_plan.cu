@@ -37,20 +37,18 @@ namespace {
 
 // Rows with more dependencies get a LONG record.  A SHORT record holding a
 // single row of kLongDeps dependencies must fit a ring slot:
-// 16 + 4*4 + 2*8*4 + kLongDeps*4*12 <= kTriSlotBytes.
+// header + 4*4 + 2*8*4 + kLongDeps*4*12 <= kTriSlotBytes.
 constexpr int kLongDeps = 32;
-static_assert(16 + 16 + 64 + kLongDeps * 4 * 12 <= kTriSlotBytes, "record slot too small");
-
-inline long long align16(long long b) { return (b + 15) & ~15LL; }
+static_assert(kRecHdrBytes + 16 + 64 + kLongDeps * 4 * 12 <= kTriSlotBytes, "record slot too small");
 
 // bytes of a SHORT record with `rows` rows of up to `len` dependencies
 inline long long rec_size(int rows, int len, int S) {
   const long long R4 = (rows + 3) & ~3;
-  return 16 + 4 * R4 + 2LL * S * R4 + (long long)len * R4 * (4 + S);
+  return kRecHdrBytes + 4 * R4 + 2LL * S * R4 + (long long)len * R4 * (4 + S);
 }
 
 struct RecDesc {
-  int tile_level_end;  // 1 when this record closes its level
+  int wait_for;  // records of the tile in earlier levels (all must be done first)
   bool is_long;
   int len;
   std::vector<int> rows;
@@ -81,9 +79,10 @@ void layout(const TriDeps& d, const std::vector<RecDesc>& recs, int S, std::vect
     hdr[1] = r.len;
     hdr[2] = r.is_long ? kRecLong : 0;
     hdr[3] = 0;
-    int* rows = hdr + 4;
+    hdr[4] = r.wait_for;
+    int* rows = hdr + kRecHdrBytes / 4;
     for (long long t = 0; t < R4; ++t) rows[t] = t < nrows ? r.rows[t] : -1;
-    const long long diag_el = (base + 16 + 4 * R4) / S;  // element index of diag[0]
+    const long long diag_el = (base + kRecHdrBytes + 4 * R4) / S;  // element index of diag[0]
     for (int t = 0; t < nrows; ++t) {
       ddst.push_back(diag_el + t);
       idst.push_back(diag_el + R4 + t);
@@ -99,8 +98,8 @@ void layout(const TriDeps& d, const std::vector<RecDesc>& recs, int S, std::vect
         }
       continue;
     }
-    int* cols = reinterpret_cast<int*>(buf.data() + base + 16 + 4 * R4 + 2 * S * R4);
-    const long long vals_el = (base + 16 + 4 * R4 + 2 * S * R4 + 4LL * r.len * R4) / S;
+    int* cols = reinterpret_cast<int*>(buf.data() + base + kRecHdrBytes + 4 * R4 + 2 * S * R4);
+    const long long vals_el = (base + kRecHdrBytes + 4 * R4 + 2 * S * R4 + 4LL * r.len * R4) / S;
     for (long long q = 0; q < (long long)r.len * R4; ++q) cols[q] = -1;
     for (int t = 0; t < nrows; ++t) {
       const int row = r.rows[t];
@@ -196,15 +195,16 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
     bucket.resize(t1 - t0);
     std::vector<int> fill(bptr.begin(), bptr.end() - 1);
     for (int i = t0; i < t1; ++i) bucket[fill[llev[i - t0]]++] = i;
+    const size_t tile_first = recs.size();
     for (int l = 0; l < nl; ++l) {
       std::vector<int> rows(bucket.begin() + bptr[l], bucket.begin() + bptr[l + 1]);
       // longest first, so records group rows of similar length
       std::stable_sort(rows.begin(), rows.end(), [&](int a, int b) { return deps_of(a) > deps_of(b); });
-      const size_t first_rec = recs.size();
+      const int wait_for = (int)(recs.size() - tile_first);  // every earlier level of the tile
       size_t p = 0;
       while (p < rows.size() && deps_of(rows[p]) > kLongDeps) {
         RecDesc r;
-        r.tile_level_end = 0;
+        r.wait_for = wait_for;
         r.is_long = true;
         r.len = deps_of(rows[p]);
         r.rows = {rows[p]};
@@ -213,7 +213,7 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
       }
       while (p < rows.size()) {
         RecDesc r;
-        r.tile_level_end = 0;
+        r.wait_for = wait_for;
         r.is_long = false;
         r.len = deps_of(rows[p]);
         r.rows.push_back(rows[p++]);  // a SHORT row (<= kLongDeps deps) always fits a slot
@@ -224,7 +224,6 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
         }
         recs.push_back(r);
       }
-      (void)first_rec;
     }
     tile_rec.push_back((int)recs.size());
   }
