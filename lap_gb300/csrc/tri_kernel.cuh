@@ -171,29 +171,41 @@ __device__ __forceinline__ T dep_value(const TriArgs<T>& A, const T* sy, int c, 
 __device__ __forceinline__ void st_shared_volatile(double* p, double v) { *(volatile double*)p = v; }
 __device__ __forceinline__ void st_shared_volatile(float* p, float v) { *(volatile float*)p = v; }
 
-// Waits (warp-uniform, lane 0 polls) until `need` records of the current
-// tile are complete, i.e. every earlier tile-level of this record is done.
+// Tile-local completion counter: release by the finishing warp, acquire by
+// the waiting one (shared memory, CTA scope -- no full fence needed).
+__device__ __forceinline__ int ld_acquire_cta(const int* p) {
+  int v;
+  asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_release_cta_add(int* p, int v) {
+  asm volatile("red.release.cta.shared::cta.add.s32 [%0], %1;" ::"r"(smem_u32(p)), "r"(v) : "memory");
+}
+
+// Waits (warp-uniform) until `need` records of the current tile are
+// complete, i.e. every earlier tile-level of this record is done.
 static __device__ __noinline__ void wait_level_slow(const int* s_done, int need, int* err) {
   SpinClock clk;
   for (unsigned polls = 1;; ++polls) {
-    if (*(const volatile int*)s_done >= need) return;
+    if (ld_acquire_cta(s_done) >= need) return;
     if ((polls & 255u) == 0u && clk.expired(err)) return;
   }
 }
-__device__ __forceinline__ void wait_level(const int* s_done, int need, int* err, int lane) {
+__device__ __forceinline__ void wait_level(const int* s_done, int need, int* err) {
   if (need <= 0) return;
-  if (lane == 0 && *(const volatile int*)s_done < need) wait_level_slow(s_done, need, err);
-  __syncwarp();
-  __threadfence_block();
+  // every lane polls the same word (a broadcast read): no warp sync needed
+  if (ld_acquire_cta(s_done) < need) wait_level_slow(s_done, need, err);
 }
 
 // Solves one staged record with one warp (lane = row of the record; a LONG
-// record's single row is split across the warp).  The rhs is formed first
-// (its loads and FP64 updates are independent of the dependencies), then the
-// warp waits for the record's earlier tile-levels, reads tile-local values
-// from shared memory and other tiles' values from global memory (read early,
-// re-read with backoff only if not yet produced), and finally counts itself
-// complete.
+// record's single row is split across the warp).  Everything that does not
+// depend on the record's inputs is done before the wait: the rhs (its loads
+// and FP64 vector updates), the record's indices and values, the early reads
+// of other tiles' values.  After the wait only the tile-local values are
+// read (one round of shared-memory loads) and the FMA chain runs; the
+// completion is published before the global stores.
+constexpr int kTriHeld = 4;  // dependencies held in registers per row
+
 template <typename T, bool EXACT, typename OP>
 __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy, int t0, int t1,
                                              const unsigned char* rec, int lane, int* s_done) {
@@ -213,19 +225,28 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
   }
   const int* cols = reinterpret_cast<const int*>(dinv + R4);
   const T* vals = reinterpret_cast<const T*>(cols + (size_t)h.len * R4);
-  constexpr int kEarly = 4;
-  T early[kEarly];
+  int hc[kTriHeld];
+  T hl[kTriHeld], hv[kTriHeld];
+  const bool short_act = !lng && act;
 #pragma unroll
-  for (int k = 0; k < kEarly; ++k) {
-    early[k] = sentinel<T>();
-    if (!lng && act && k < h.len) {
+  for (int k = 0; k < kTriHeld; ++k) {
+    hc[k] = -1;
+    hv[k] = sentinel<T>();
+    hl[k] = T(0);
+    if (short_act && k < h.len) {
       const int c = cols[k * R4 + lane];
-      if (c >= 0 && (c < t0 || c >= t1)) early[k] = ld_relaxed(A.y + c);
+      hc[k] = c;
+      if (c >= 0) {
+        hl[k] = vals[k * R4 + lane];
+        if (c < t0 || c >= t1) hv[k] = ld_relaxed(A.y + c);  // other tile: read early
+      }
     }
   }
+  const T dg = short_act ? (EXACT ? diag[lane] : dinv[lane]) : T(0);
   T acc = T(0);
   if (act && (!lng || lane == 0)) acc = op.rhs(row, pr);
-  wait_level(s_done, h.wait_for, A.err, lane);
+  wait_level(s_done, h.wait_for, A.err);
+  T yv = T(0);
   if (lng) {
     T s = T(0);
     for (int k = lane; k < h.len; k += 32) {
@@ -236,35 +257,38 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
     s = warp_sum(s);
     if (lane == 0) {
       const T r = sub_rn(acc, s);
-      const T yv = publishable(EXACT ? div_rn(r, diag[0]) : r * dinv[0]);
+      yv = publishable(EXACT ? div_rn(r, diag[0]) : r * dinv[0]);
       sy[row - t0] = yv;
-      st_relaxed(A.y + row, yv);
-      op.done(row, yv, dp);
     }
   } else if (act) {
+    // tile-local values: complete (earlier tile-levels); all loads at once
+#pragma unroll
+    for (int k = 0; k < kTriHeld; ++k)
+      if (hc[k] >= t0 && hc[k] < t1) hv[k] = sy[hc[k] - t0];
     // the reference's order: acc = rhs; acc -= l_k * y_k for k ascending
-    for (int k = 0; k < h.len; ++k) {
+#pragma unroll
+    for (int k = 0; k < kTriHeld; ++k) {
+      if (hc[k] >= 0) {
+        T v = hv[k];
+        if (is_sentinel(v)) v = wait_value_slow(A.y + hc[k], A.err);  // other tile, not yet written
+        acc = EXACT ? sub_rn(acc, mul_rn(hl[k], v)) : fma_rn(-hl[k], v, acc);
+      }
+    }
+    for (int k = kTriHeld; k < h.len; ++k) {
       const int c = cols[k * R4 + lane];
       if (c < 0) break;
       const T l = vals[k * R4 + lane];
-      T v;
-      if (c >= t0 && c < t1) {
-        v = sy[c - t0];  // an earlier tile-level: complete
-      } else {
-        v = k < kEarly ? early[k] : sentinel<T>();
-        if (is_sentinel(v)) v = wait_value_slow(A.y + c, A.err);
-      }
+      const T v = (c >= t0 && c < t1) ? sy[c - t0] : dep_value(A, sy, c, t0, t1);
       acc = EXACT ? sub_rn(acc, mul_rn(l, v)) : fma_rn(-l, v, acc);
     }
-    const T yv = publishable(EXACT ? div_rn(acc, diag[lane]) : acc * dinv[lane]);
+    yv = publishable(EXACT ? div_rn(acc, dg) : acc * dg);
     sy[row - t0] = yv;
-    st_relaxed(A.y + row, yv);
-    op.done(row, yv, dp);
   }
   __syncwarp();
-  if (lane == 0) {
-    __threadfence_block();
-    atomicAdd(s_done, 1);
+  if (lane == 0) red_release_cta_add(s_done, 1);
+  if (act && (!lng || lane == 0)) {
+    st_relaxed(A.y + row, yv);
+    op.done(row, yv, dp);
   }
 }
 
