@@ -86,7 +86,12 @@ struct TriPlan {
   int *tile_row0 = nullptr, *tile_row1 = nullptr;  // [ntiles], processing order
   int *tile_rec = nullptr;   // [ntiles+1]
   int *rec_flags = nullptr;  // [nrec]
+  // r64: the factor's values as stored (the exact solves).  buf64s (FP64)
+  // and r32 (FP32) hold the FMA form used inside the PCG: entry values
+  // pre-multiplied by the reciprocal of their row's diagonal.  buf64s shares
+  // r64's layout and offsets.
   RecordSet r64, r32;
+  unsigned char* buf64s = nullptr;
   int nval = 0, ndiag = 0, nlong = 0;
   int *vsrc = nullptr;       // [nval] index of each entry value in the value source array
   int *dsrc = nullptr;       // [ndiag] index of each diagonal in the diagonal source array

@@ -284,6 +284,13 @@ struct OpPcgLower {
   __device__ void done(int i, T, const DPre&) {
     if (sfill) sfill[i] = sentinel<T>();
   }
+  __device__ void prefetch(int r0, int r1, int part) const {
+    prefetch_rows_l2(r, r0, r1, part, kTriProdLanes);
+    if (!do_update) return;
+    prefetch_rows_l2(x, r0, r1, part, kTriProdLanes);
+    prefetch_rows_l2(p, r0, r1, part, kTriProdLanes);
+    prefetch_rows_l2(q, r0, r1, part, kTriProdLanes);
+  }
   __device__ void chunk_end(int c, int nchunks, unsigned* ticket, double* sm) {
     double v[1] = {rr};
     rr = 0.0;
@@ -353,6 +360,10 @@ struct OpIcUpper {
   __device__ T rhs(int, const Pre& v) const { return v.t; }
   __device__ DPre dpre(int i) const { return {r[i]}; }
   __device__ void done(int, T y, const DPre& v) { rho += (double)v.r * (double)y; }
+  __device__ void prefetch(int r0, int r1, int part) const {
+    prefetch_rows_l2(t, r0, r1, part, kTriProdLanes);
+    prefetch_rows_l2(r, r0, r1, part, kTriProdLanes);
+  }
   __device__ void chunk_end(int c, int nchunks, unsigned* ticket, double* sm) {
     rho_chunk_end(rho, st, part, c, nchunks, ticket, sm);
   }
@@ -396,6 +407,11 @@ struct OpGsUpper {
     const T wi = v.t + y;
     w[i] = wi;
     rho += (double)v.r * (double)wi;
+  }
+  __device__ void prefetch(int r0, int r1, int part) const {
+    prefetch_rows_l2(t, r0, r1, part, kTriProdLanes);
+    prefetch_rows_l2(r, r0, r1, part, kTriProdLanes);
+    prefetch_rows_l2(ia, r0, r1, part, kTriProdLanes);
   }
   __device__ void chunk_end(int c, int nchunks, unsigned* ticket, double* sm) {
     rho_chunk_end(rho, st, part, c, nchunks, ticket, sm);
@@ -579,7 +595,7 @@ static int launch_lower(gb_system sys, PcgState* st, int do_update, cudaGraphCon
   op.cond = cond;
   op.has_cond = has_cond;
   op.do_update = do_update;
-  return tri_launch<T, OpPcgLower<T>, false>(sys->L, tri_args<T>(sys->L, v.t, sys->err), op, sys->s);
+  return tri_launch<T, OpPcgLower<T>, false>(sys->L, tri_args<T>(sys->L, v.t, sys->err, true), op, sys->s);
 }
 
 template <typename T>
@@ -587,10 +603,10 @@ static int launch_upper(gb_system sys, PcgState* st) {
   auto v = vecs<T>(sys);
   if (sys->prec == GB_PREC_ICHOL) {
     OpIcUpper<T> op{v.t, v.r, st, sys->part, false, 0.0};
-    return tri_launch<T, OpIcUpper<T>, false>(sys->U, tri_args<T>(sys->U, v.s, sys->err), op, sys->s);
+    return tri_launch<T, OpIcUpper<T>, false>(sys->U, tri_args<T>(sys->U, v.s, sys->err, true), op, sys->s);
   }
   OpGsUpper<T> op{v.t, v.r, sys->ia, sys->ja, mat_vals<T>(sys), v.w, st, sys->part, false, 0.0};
-  return tri_launch<T, OpGsUpper<T>, false>(sys->U, tri_args<T>(sys->U, v.s, sys->err), op, sys->s);
+  return tri_launch<T, OpGsUpper<T>, false>(sys->U, tri_args<T>(sys->U, v.s, sys->err, true), op, sys->s);
 }
 
 // w buffer the spmv_pq kernel gathers: ichol's w is the upper solve's output

@@ -97,21 +97,21 @@ int apply_prec_composed(gb_system sys, const double* in, double* out) {
       for (int i = 0; i < sys->k; ++i) {
         GB_TRY(copy_dev(n, in, v2, st));
         GB_TRY(spmv_A(sys, out, v2, -1.0, 1.0));
-        GB_TRY(tri_solve_plain<double>(&sys->L, v2, v1, sys->err, st));
+        GB_TRY(tri_solve_plain(&sys->L, v2, v1, sys->err, st));
         GB_TRY(axpy_dev(n, 1.0, v1, out, st));
       }
       for (int i = 0; i < sys->k; ++i) {
         GB_TRY(copy_dev(n, in, v2, st));
         GB_TRY(spmv_A(sys, out, v2, -1.0, 1.0));
-        GB_TRY(tri_solve_plain<double>(&sys->U, v2, v1, sys->err, st));
+        GB_TRY(tri_solve_plain(&sys->U, v2, v1, sys->err, st));
         GB_TRY(axpy_dev(n, 1.0, v1, out, st));
       }
       return GB_OK;
     }
     case GB_PREC_ICHOL:
       // simple_blas.c:200-221: L^{-1} then (L^T)^{-1}
-      GB_TRY(tri_solve_plain<double>(&sys->L, in, v1, sys->err, st));
-      return tri_solve_plain<double>(&sys->U, v1, out, sys->err, st);
+      GB_TRY(tri_solve_plain(&sys->L, in, v1, sys->err, st));
+      return tri_solve_plain(&sys->U, v1, out, sys->err, st);
   }
   return GB_BAD_INPUT;
 }

@@ -38,13 +38,14 @@ int tri_grid(int ntiles);
 int tri_blocks_per_sm();
 void tri_set_blocks_per_sm(int bps);
 void tri_plan_free(TriPlan* plan);
-// eval/diag (and their FP32 copies when want32) from value arrays.
-int tri_plan_fill(TriPlan* plan, const double* ent_src, const double* diag_src, bool want32,
+// Writes the record values from value arrays: the exact FP64 records and,
+// when for_pcg, the FMA-form FP64 and FP32 records the PCG solves read.
+int tri_plan_fill(TriPlan* plan, const double* ent_src, const double* diag_src, bool for_pcg,
                   cudaStream_t s);
 
-// y = T^{-1} x with the plan's values.  y must not alias x.
-template <typename T>
-int tri_solve_plain(const TriPlan* plan, const T* x, T* y, int* err, cudaStream_t s);
+// y = T^{-1} x with the plan's values, rounded as the reference rounds.  y
+// must not alias x.
+int tri_solve_plain(const TriPlan* plan, const double* x, double* y, int* err, cudaStream_t s);
 
 // IC(0) factorization on A's pattern (left-looking, sync-free, level order
 // of the lower schedule).  f receives the factor in symmetric storage: the

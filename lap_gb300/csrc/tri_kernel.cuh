@@ -4,17 +4,19 @@
 // row is solved as simple_lower/upper_triangular_solve (simple_blas.c:46-85)
 // does: acc = rhs; acc -= l_ij * y_j in the row's column order; y_i = acc /
 // d_i.  EXACT keeps that rounding (separate mul and sub, a true division);
-// otherwise the row uses FMAs and the precomputed reciprocal of d_i -- GB300
-// runs FP64 at 1/64 of its FP32 rate, so every FP64 instruction on the
-// dependency chain counts.
+// otherwise the row computes y_i = rhs/d_i - sum (l_ij/d_i) y_j with FMAs and
+// the precomputed reciprocal of d_i, and does the scaling (and the terms
+// whose y_j is already available) before it waits -- GB300 runs FP64 at 1/64
+// of its FP32 rate, so every FP64 instruction on the dependency chain counts.
 //
 // Schedule (TriPlan, built on the host): rows are cut into contiguous tiles;
 // inside a tile rows are ordered by their level with respect to the tile's
 // own rows and packed into RECORDS of at most 32 rows of one level (rows,
 // diagonal, its reciprocal, dependency columns and values column-major;
 // contiguous and 16-byte aligned).  One CTA solves one tile at a time:
-//   * a producer warp streams the tile's records, in order, into a ring of
-//     shared-memory slots with cp.async.bulk (TMA), one mbarrier per slot;
+//   * a producer warp streams the tile's records into a ring of shared-
+//     memory slots with cp.async.bulk (TMA), one mbarrier per slot, several
+//     lanes issuing copies in parallel;
 //   * consumer warps take the records round-robin, one row per lane.  A
 //     dependency inside the tile is read from the tile's solution array in
 //     shared memory, spinning while it still holds the sentinel; one in an
@@ -35,6 +37,9 @@
 //   T rhs(int row, const Pre&)      rhs value (may store updated vectors)
 //   DPre dpre(int row)              loads for the epilogue
 //   void done(int row, T y, const DPre&)
+//   void prefetch(int r0, int r1, int part)   producer lane `part` (of
+//        kTriProdLanes), once per tile: L2 prefetch of its share of the
+//        vectors pre()/dpre() read over the tile's rows [r0, r1)
 //   void chunk_end(tile_ix, ntiles, ticket, sm)   whole block, after the
 //        tile; ticket[1] counts finished tiles (chunk_finished()).
 #pragma once
@@ -50,6 +55,8 @@ constexpr int kTriThreads = (kTriConsumers + 1) * 32;  // + one producer warp
 constexpr int kTriSlots = 40;                          // ring depth (records in flight)
 constexpr int kTriSlotBytes = 2048;                    // max record size
 constexpr int kTriL2Ahead = 32;                        // records prefetched into L2 ahead of the ring
+constexpr int kTriProdLanes = 8;                       // producer lanes issuing copies in parallel
+static_assert(kTriSlots % kTriProdLanes == 0, "a slot is always refilled by the same producer lane");
 constexpr int kTriRecTable = 1024;                     // records of a tile cached in smem
 constexpr int kTriRecRows = 32;                        // rows per record (one per lane)
 constexpr int kRecLong = 2;                            // record flag: one row, warp-reduced
@@ -135,6 +142,22 @@ __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned
           smem_u32(dst)),
       "l"(src), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
+}
+
+// L2 prefetch of piece `part` of `nparts` of v[r0 .. r1): a hint, so the
+// range is shrunk to whole 16-byte units inside it (the bulk prefetch's
+// alignment rule) and never reaches outside the rows asked for.
+template <typename T>
+__device__ __forceinline__ void prefetch_rows_l2(const T* v, int r0, int r1, int part, int nparts) {
+  if (v == nullptr || r1 <= r0) return;
+  const uintptr_t a = ((uintptr_t)(v + r0) + 15u) & ~(uintptr_t)15u;
+  const uintptr_t b = (uintptr_t)(v + r1) & ~(uintptr_t)15u;
+  if (b <= a) return;
+  const uintptr_t piece = (((b - a) + nparts - 1) / nparts + 15u) & ~(uintptr_t)15u;
+  const uintptr_t s0 = a + (uintptr_t)part * piece;
+  if (s0 >= b) return;
+  const uintptr_t n = (b - s0) < piece ? (b - s0) : piece;
+  tma_prefetch_l2(reinterpret_cast<const void*>(s0), (unsigned)n);
 }
 
 // Spin on a tile-local value in shared memory (written by another warp of
@@ -245,6 +268,26 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
   const T dg = short_act ? (EXACT ? diag[lane] : dinv[lane]) : T(0);
   T acc = T(0);
   if (act && (!lng || lane == 0)) acc = op.rhs(row, pr);
+  bool pend[kTriHeld];
+#pragma unroll
+  for (int k = 0; k < kTriHeld; ++k) pend[k] = hc[k] >= 0;
+  if (!EXACT && short_act) {
+    // FMA-form records hold l/d: y = rhs/d - sum (l/d) y_dep.  The scaling
+    // and the held dependencies in earlier tiles (read early; complete or
+    // awaited here, independent of this tile's progress) leave the chain that
+    // runs after the wait.  The order -- other tiles' terms first, then this
+    // tile's, each in column order -- does not depend on timing, so results
+    // are reproducible.
+    acc = acc * dg;
+#pragma unroll
+    for (int k = 0; k < kTriHeld; ++k) {
+      if (pend[k] && (hc[k] < t0 || hc[k] >= t1)) {
+        const T v = is_sentinel(hv[k]) ? wait_value_slow(A.y + hc[k], A.err) : hv[k];
+        acc = fma_rn(-hl[k], v, acc);
+        pend[k] = false;
+      }
+    }
+  }
   wait_level(s_done, h.wait_for, A.err);
   T yv = T(0);
   if (lng) {
@@ -264,11 +307,11 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
     // tile-local values: complete (earlier tile-levels); all loads at once
 #pragma unroll
     for (int k = 0; k < kTriHeld; ++k)
-      if (hc[k] >= t0 && hc[k] < t1) hv[k] = sy[hc[k] - t0];
+      if (pend[k] && hc[k] >= t0 && hc[k] < t1) hv[k] = sy[hc[k] - t0];
     // the reference's order: acc = rhs; acc -= l_k * y_k for k ascending
 #pragma unroll
     for (int k = 0; k < kTriHeld; ++k) {
-      if (hc[k] >= 0) {
+      if (pend[k]) {
         T v = hv[k];
         if (is_sentinel(v)) v = wait_value_slow(A.y + hc[k], A.err);  // other tile, not yet written
         acc = EXACT ? sub_rn(acc, mul_rn(hl[k], v)) : fma_rn(-hl[k], v, acc);
@@ -281,7 +324,7 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
       const T v = (c >= t0 && c < t1) ? sy[c - t0] : dep_value(A, sy, c, t0, t1);
       acc = EXACT ? sub_rn(acc, mul_rn(l, v)) : fma_rn(-l, v, acc);
     }
-    yv = publishable(EXACT ? div_rn(acc, dg) : acc * dg);
+    yv = publishable(EXACT ? div_rn(acc, dg) : acc);
     sy[row - t0] = yv;
   }
   __syncwarp();
@@ -300,7 +343,7 @@ __global__ void __launch_bounds__(kTriThreads, 1) tri_tile_kernel(TriArgs<T> A, 
   __shared__ __align__(8) uint64_t full_bar[kTriSlots], empty_bar[kTriSlots];
   __shared__ long long s_roff[kTriRecTable];
   __shared__ int s_rbytes[kTriRecTable];
-  __shared__ unsigned s_issued;
+  __shared__ unsigned s_last_u[kTriSlots];  // last record (stream index) copied into each slot
   __shared__ int s_tile;
   __shared__ int s_done;  // records of the current tile completed
   __shared__ double s_red[64];
@@ -315,12 +358,12 @@ __global__ void __launch_bounds__(kTriThreads, 1) tri_tile_kernel(TriArgs<T> A, 
     for (int s = 0; s < kTriSlots; ++s) {
       mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
+      s_last_u[s] = ~0u;
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
   unsigned base = 0;       // records of earlier tiles streamed by this CTA
-  unsigned issued = 0;     // producer: records issued (all tiles)
   bool failed = false;
   while (true) {
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(&A.ticket[0], 1u);
@@ -339,11 +382,15 @@ __global__ void __launch_bounds__(kTriThreads, 1) tri_tile_kernel(TriArgs<T> A, 
     if (threadIdx.x == 0) s_done = 0;
     __syncthreads();
     if (producer) {
-      if (lane == 0) {
-        for (int q = 0; q < nrec && !failed; ++q, ++issued) {
+      // lane j streams records j, j+L, j+2L, ... (L = kTriProdLanes): the
+      // issue of a bulk copy costs about an L2 round trip, so one lane alone
+      // would deliver records slower than the consumers solve them.  Slot
+      // u % kTriSlots is refilled by the lane that filled it before.
+      if (lane < kTriProdLanes) {
+        for (int q = lane, n = 1; q < nrec && !failed; q += kTriProdLanes, ++n) {
           const unsigned u = base + q;
           const int slot = u % kTriSlots;
-          if ((q & 15) == 15 && ld_volatile(A.err) != 0) {
+          if ((n & 15) == 0 && ld_volatile(A.err) != 0) {
             failed = true;
             break;
           }
@@ -355,6 +402,10 @@ __global__ void __launch_bounds__(kTriThreads, 1) tri_tile_kernel(TriArgs<T> A, 
           const long long off = q < kTriRecTable ? s_roff[q] : __ldg(A.rec_off + rec0 + q);
           mbar_expect_tx(&full_bar[slot], bytes);
           tma_load_1d(ring + slot * kTriSlotBytes, A.recbuf + off, bytes, &full_bar[slot]);
+          s_last_u[slot] = u;
+          // after the first record is on its way: warm L2 with the vectors
+          // this tile's rows read (HBM latency off the records' path)
+          if (n == 1) op.prefetch(t0, t1, lane);
           // warm L2 with a record further ahead, so ring copies hit L2
           const int qa = q + kTriL2Ahead;
           if (qa < nrec && qa < kTriRecTable) tma_prefetch_l2(A.recbuf + s_roff[qa], (unsigned)s_rbytes[qa]);
@@ -379,15 +430,16 @@ __global__ void __launch_bounds__(kTriThreads, 1) tri_tile_kernel(TriArgs<T> A, 
     __syncthreads();
   }
   // Drain: every issued copy must have landed before the CTA's shared
-  // memory goes away.  A slot is reused only after its previous record was
-  // consumed, so only the last ring window of issues can still be in
-  // flight (after a timeout); wait for those, bounded.
-  if (threadIdx.x == kTriConsumers * 32) s_issued = issued;
+  // memory goes away.  A slot is refilled only after its previous record was
+  // consumed, so only the last copy into each slot can still be in flight
+  // (after a timeout); wait for those, bounded.  A completed copy's phase is
+  // the barrier's current or immediately preceding one, so the wait on its
+  // parity returns at once.
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned last = s_issued;
-    for (unsigned u = last > (unsigned)kTriSlots ? last - kTriSlots : 0u; u < last; ++u) {
-      const int slot = u % kTriSlots;
+    for (int slot = 0; slot < kTriSlots; ++slot) {
+      const unsigned u = s_last_u[slot];
+      if (u == ~0u) continue;
       const uint64_t w0 = globaltimer_ns();
       while (!mbar_try_wait(&full_bar[slot], (u / kTriSlots) & 1u) &&
              globaltimer_ns() - w0 < kSpinBudgetNs) {
@@ -436,8 +488,10 @@ int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   return GB_OK;
 }
 
+// fma_form: FP64 solves read the FMA-form records (the PCG); FP32 solves
+// always do.  The exact (EXACT) solves pass false.
 template <typename T>
-TriArgs<T> tri_args(const TriPlan& p, T* y, int* err);
+TriArgs<T> tri_args(const TriPlan& p, T* y, int* err, bool fma_form);
 
 // Plain solve: rhs from an input vector.
 template <typename T>
@@ -454,6 +508,9 @@ struct OpPlain {
   __device__ __forceinline__ T rhs(int, const Pre& p) const { return p.x; }
   __device__ __forceinline__ DPre dpre(int) const { return {}; }
   __device__ __forceinline__ void done(int, T, const DPre&) {}
+  __device__ __forceinline__ void prefetch(int r0, int r1, int part) const {
+    prefetch_rows_l2(x, r0, r1, part, kTriProdLanes);
+  }
   __device__ __forceinline__ void chunk_end(int, int nchunks, unsigned* ticket, double*) {
     if (threadIdx.x == 0) chunk_finished(ticket, nchunks);
   }

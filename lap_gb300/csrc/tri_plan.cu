@@ -273,6 +273,7 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
 void tri_plan_free(TriPlan* p) {
   free_set(&p->r64);
   free_set(&p->r32);
+  if (p->buf64s) cudaFree(p->buf64s);
   void* ptrs[] = {p->tile_row0, p->tile_row1, p->tile_rec, p->rec_flags, p->vsrc,
                   p->dsrc,      p->long_col,  p->long_src, p->order,     p->ticket};
   for (void* q : ptrs)
@@ -299,7 +300,36 @@ __global__ void fill_records_kernel(int nval, const long long* __restrict__ vdst
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nlong; i += stride) lval[i] = (T)ent[lsrc[i]];
 }
 
-int tri_plan_fill(TriPlan* p, const double* ent_src, const double* diag_src, bool want32,
+// FMA form: every short record's entry values times the reciprocal of their
+// row's diagonal, computed in FP64 from the exact records and written to the
+// FP64 copy (which already holds the rest of the record) and rounded once to
+// the FP32 records.  One warp per record, one lane per row.
+__global__ void scale_records_kernel(int nrec, const long long* __restrict__ off64,
+                                     const unsigned char* __restrict__ buf64,
+                                     const long long* __restrict__ off32, unsigned char* buf32,
+                                     unsigned char* buf64s) {
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int rec = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); rec < nrec; rec += warps) {
+    const unsigned char* r = buf64 + off64[rec];
+    const RecHdr h = *reinterpret_cast<const RecHdr*>(r);
+    if ((h.flags & kRecLong) != 0 || lane >= h.nrows) continue;
+    const int R4 = (h.nrows + 3) & ~3;
+    const size_t vals64 = sizeof(RecHdr) + (size_t)R4 * (4 + 8 + 8) + (size_t)h.len * R4 * 4;
+    const size_t vals32 = sizeof(RecHdr) + (size_t)R4 * (4 + 4 + 4) + (size_t)h.len * R4 * 4;
+    const double dinv = reinterpret_cast<const double*>(r + sizeof(RecHdr) + (size_t)R4 * 12)[lane];
+    const double* v = reinterpret_cast<const double*>(r + vals64);
+    double* vs = reinterpret_cast<double*>(buf64s + off64[rec] + vals64);
+    float* v32 = reinterpret_cast<float*>(buf32 + off32[rec] + vals32);
+    for (int k = 0; k < h.len; ++k) {
+      const double x = v[k * R4 + lane] * dinv;
+      vs[k * R4 + lane] = x;
+      v32[k * R4 + lane] = (float)x;
+    }
+  }
+}
+
+int tri_plan_fill(TriPlan* p, const double* ent_src, const double* diag_src, bool for_pcg,
                   cudaStream_t s) {
   const int g = std::max(1, std::min(device_sm_count() * 8, ceil_div(std::max(p->nval, p->ndiag), 256)));
   fill_records_kernel<double><<<g, 256, 0, s>>>(p->nval, p->r64.vdst, p->vsrc, ent_src, p->ndiag,
@@ -307,12 +337,20 @@ int tri_plan_fill(TriPlan* p, const double* ent_src, const double* diag_src, boo
                                                 p->nlong, p->long_src, (double*)p->r64.buf,
                                                 (double*)p->r64.long_val);
   GB_CUDA_TRY(cudaGetLastError());
-  if (want32) {
+  if (for_pcg) {
     fill_records_kernel<float><<<g, 256, 0, s>>>(p->nval, p->r32.vdst, p->vsrc, ent_src, p->ndiag,
                                                  p->r32.ddst, p->r32.idst, p->dsrc, diag_src,
                                                  p->nlong, p->long_src, (float*)p->r32.buf,
                                                  (float*)p->r32.long_val);
     GB_CUDA_TRY(cudaGetLastError());
+    if (!p->buf64s) GB_CUDA_TRY(cudaMalloc(&p->buf64s, (size_t)p->r64.bytes));
+    GB_CUDA_TRY(cudaMemcpyAsync(p->buf64s, p->r64.buf, (size_t)p->r64.bytes, cudaMemcpyDeviceToDevice, s));
+    if (p->nrec > 0) {
+      const int gs = std::max(1, std::min(device_sm_count() * 8, ceil_div(p->nrec, 8)));
+      scale_records_kernel<<<gs, 256, 0, s>>>(p->nrec, p->r64.off, p->r64.buf, p->r32.off, p->r32.buf,
+                                              p->buf64s);
+      GB_CUDA_TRY(cudaGetLastError());
+    }
     p->have32 = true;
   }
   return GB_OK;
@@ -337,7 +375,7 @@ int tri_grid(int ntiles) {
 }
 
 template <typename T>
-TriArgs<T> tri_args(const TriPlan& p, T* y, int* err) {
+TriArgs<T> tri_args(const TriPlan& p, T* y, int* err, bool fma_form) {
   const RecordSet& rs = sizeof(T) == 8 ? p.r64 : p.r32;
   TriArgs<T> A;
   A.ntiles = p.ntiles;
@@ -346,7 +384,7 @@ TriArgs<T> tri_args(const TriPlan& p, T* y, int* err) {
   A.tile_rec = p.tile_rec;
   A.rec_off = rs.off;
   A.rec_bytes = rs.nbytes;
-  A.recbuf = rs.buf;
+  A.recbuf = (sizeof(T) == 8 && fma_form) ? p.buf64s : rs.buf;
   A.long_col = p.long_col;
   A.long_val = (const T*)rs.long_val;
   A.y = y;
@@ -355,17 +393,14 @@ TriArgs<T> tri_args(const TriPlan& p, T* y, int* err) {
   A.tile_rows = p.tile_rows;
   return A;
 }
-template TriArgs<double> tri_args<double>(const TriPlan&, double*, int*);
-template TriArgs<float> tri_args<float>(const TriPlan&, float*, int*);
+template TriArgs<double> tri_args<double>(const TriPlan&, double*, int*, bool);
+template TriArgs<float> tri_args<float>(const TriPlan&, float*, int*, bool);
 
-template <typename T>
-int tri_solve_plain(const TriPlan* p, const T* x, T* y, int* err, cudaStream_t s) {
+int tri_solve_plain(const TriPlan* p, const double* x, double* y, int* err, cudaStream_t s) {
   if (p->n <= 0) return GB_OK;
   GB_TRY(fill_sentinel_dev(p->n, y, s));
-  OpPlain<T> op{x};
-  return tri_launch<T, OpPlain<T>, true>(*p, tri_args<T>(*p, y, err), op, s);
+  OpPlain<double> op{x};
+  return tri_launch<double, OpPlain<double>, true>(*p, tri_args<double>(*p, y, err, false), op, s);
 }
-template int tri_solve_plain<double>(const TriPlan*, const double*, double*, int*, cudaStream_t);
-template int tri_solve_plain<float>(const TriPlan*, const float*, float*, int*, cudaStream_t);
 
 }  // namespace gb
