@@ -167,6 +167,31 @@ int gb_profile_iteration(gb_system sys, const double *b, double *x, int precisio
                          char *names_host, int names_len, double *ms_host,
                          double *bytes_host, int max_kernels, int *count);
 
+/* ------------------------------------------------------------ allocation-free dot */
+/* Largest n gb_dot_noalloc accepts (8192 partials of 4096 elements). */
+#define GB_DOT_NOALLOC_MAX_N 33554432
+
+/* *result_host = v'w for device vectors v, w of length n, without allocating
+ * any device memory.  No counterpart in LAP, whose dot() (cuda_blas.cu via
+ * blas.h) works in cuBLAS-owned memory; this library's cuda_dot()
+ * allocates its scratch on first use.  For callers that cannot let a
+ * library allocate: processes whose device memory is already claimed by
+ * another allocator (a late cudaMalloc would fail), and loops that must not
+ * risk the implicit synchronisation of cudaMalloc / cudaFree while other
+ * streams have work in flight.  The scratch (partials, completion ticket,
+ * result) lives in one fixed 64 KB array per device inside this library.
+ *   - n > GB_DOT_NOALLOC_MAX_N is rejected with GB_BAD_INPUT (and a message
+ *     on stderr) before any device work; use cuda_dot() for longer vectors.
+ *   - The first call on each device, with that device current, sets up the
+ *     scratch address (cudaGetSymbolAddress); make it before any stream
+ *     capture begins.
+ *   - Calls that can overlap on one device (several host threads, or
+ *     unordered streams) share the scratch and race: serialise them.
+ * stream: a cudaStream_t, or NULL for the legacy default stream; the call
+ * returns after the result has reached *result_host.  The rounding depends on
+ * n only (fixed chunking), and may differ from cuda_dot() in the last bits. */
+int gb_dot_noalloc(int n, const double *v, const double *w, double *result_host, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

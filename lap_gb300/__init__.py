@@ -92,6 +92,7 @@ def _proto(L: C.CDLL) -> None:
         "gb_pcg_solve_multi": (i, [vp, i, vp, vp, C.POINTER(PcgOpts), vp, C.POINTER(PcgResult)]),
         "gb_autotune_spmv": (i, [vp, C.POINTER(i)]),
         "gb_debug_set_spin_budget": (i, [vp, C.c_ulonglong]),
+        "gb_dot_noalloc": (i, [i, vp, vp, C.POINTER(C.c_double), vp]),
         "gb_profile_iteration": (i, [vp, vp, vp, i, i, C.c_char_p, i, vp, vp, i, C.POINTER(i)]),
         # LAP surface
         "cuda_dot": (d, [i, vp, vp]),
