@@ -66,8 +66,15 @@ int gb_system_info(gb_system sys, int *lower_levels, int *upper_levels, int *spm
 typedef struct {
   double tol;        /* stop when ||r|| < tol*||r0|| (cg.c:60,107); mixed: ||b-Ax|| < tol*||b-Ax0|| */
   int maxit;         /* iteration cap; like cg.c at most maxit+1 iterations run */
-  int precision;     /* 0: FP64 PCG.  1: FP32 inner PCG inside FP64 iterative refinement */
-  double inner_tol;  /* mixed: residual reduction asked of each inner solve (default 1e-4) */
+  int precision;     /* 0: FP64 PCG.
+                        1: FP32 inner PCG (FP32 Krylov vectors, SpMV and preconditioner)
+                           inside FP64 iterative refinement.
+                        2: split: FP64 Krylov vectors and scalars around an FP32 SpMV and
+                           FP32 triangular-solve preconditioner ("ichol", "GS_std" with
+                           k = 1), with FP64 residual replacement.  */
+  double inner_tol;  /* mixed: residual reduction between refinement / replacement steps;
+                        0 (default) selects 1e-4 for precision 1 and 1e-2 for precision 2.
+                        A cycle never runs past the solve's own tolerance. */
   int max_outer;     /* mixed: refinement steps cap (default 50) */
   int use_graph;     /* 1 (default): the iteration loop is one CUDA graph with a device-side
                         while node; 0: host-launched kernels, one status read per 16 iterations */

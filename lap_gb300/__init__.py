@@ -150,7 +150,7 @@ def ptr(t) -> int:
     return 0 if t is None else int(t.data_ptr())
 
 
-def opts(tol=1e-8, maxit=10000, precision=0, inner_tol=1e-4, max_outer=50, use_graph=True,
+def opts(tol=1e-8, maxit=10000, precision=0, inner_tol=0.0, max_outer=50, use_graph=True,
          verbose=False) -> PcgOpts:
     o = PcgOpts()
     lib().gb_pcg_opts_default(C.byref(o))

@@ -186,9 +186,13 @@ extern "C" int gb_profile_iteration(gb_system s, const double* b, double* x, int
   init.hist_len = s->hist_cap;
   init.flag = 1;
   PcgState* st = s->st;
+  if (precision < 0 || precision > 2) return GB_BAD_INPUT;
   if (precision == 0) {
     GB_CUDA_TRY(cudaMemcpyAsync(st, &init, sizeof init, cudaMemcpyHostToDevice, s->s));
     GB_TRY(launch_prologue<double>(s, st, 0, s->b_int));
+  } else if (precision == 2) {
+    GB_CUDA_TRY(cudaMemcpyAsync(st, &init, sizeof init, cudaMemcpyHostToDevice, s->s));
+    GB_TRY(launch_prologue_split(s, st, s->b_int));
   } else {
     PcgState o = init;
     GB_CUDA_TRY(cudaMemcpyAsync(s->st_out, &o, sizeof o, cudaMemcpyHostToDevice, s->s));
@@ -208,7 +212,9 @@ extern "C" int gb_profile_iteration(gb_system s, const double* b, double* x, int
     hook.count = 0;
     g_prof = &hook;
     cudaEventRecord(start, s->s);
-    rc = precision == 0 ? launch_body<double>(s, st, 0, 0) : launch_body<float>(s, st, 0, 0);
+    rc = precision == 0   ? launch_body<double>(s, st, 0, 0)
+         : precision == 2 ? launch_body_split(s, st, 0, 0)
+                          : launch_body<float>(s, st, 0, 0);
     g_prof = nullptr;
     if (cudaStreamSynchronize(s->s) != cudaSuccess) rc = GB_CUDA_ERROR;
     nk = hook.count;

@@ -203,7 +203,7 @@ static void tri_solve_embedded(const char* where, bool lower, int n, int nnz, co
   int rc = ensure_scratch();
   TriEntry* e = nullptr;
   if (rc == GB_OK) rc = get_tri(n, nnz, p, j, lower, &e);
-  if (rc == GB_OK) rc = tri_plan_fill(&e->plan, v, v, false, kStream);
+  if (rc == GB_OK) rc = tri_plan_fill(&e->plan, v, v, kFillExact, kStream);
   if (rc == GB_OK) rc = tri_solve_plain(&e->plan, x, y, g_s.err, kStream);
   report(where, rc);
 }
@@ -291,8 +291,8 @@ extern "C" void cuda_ichol(const int* ia, const int* ja, double* a, const int nn
   const int n = prec_data->n;
   int rc = ensure_scratch();
   if (rc == GB_OK) rc = get_ic(n, nnzA, ia, ja, &e);
-  if (rc == GB_OK) rc = tri_plan_fill(&e->lower, prec_data->ichol_vals, prec_data->ichol_vals, false, kStream);
-  if (rc == GB_OK) rc = tri_plan_fill(&e->upper, prec_data->ichol_vals, prec_data->ichol_vals, false, kStream);
+  if (rc == GB_OK) rc = tri_plan_fill(&e->lower, prec_data->ichol_vals, prec_data->ichol_vals, kFillExact, kStream);
+  if (rc == GB_OK) rc = tri_plan_fill(&e->upper, prec_data->ichol_vals, prec_data->ichol_vals, kFillExact, kStream);
   if (rc == GB_OK) rc = tri_solve_plain(&e->lower, x, prec_data->aux_vec1, g_s.err, kStream);
   if (rc == GB_OK) rc = tri_solve_plain(&e->upper, prec_data->aux_vec1, y, g_s.err, kStream);
   report("cuda_ichol", rc);

@@ -336,10 +336,11 @@ __device__ __forceinline__ void rho_chunk_end(double& rho, PcgState* st, double*
 }
 
 // Upper solve whose output is w (ichol: w = (L L^T)^-1 r), reducing r'w.
-template <typename T>
+// TR: type of the residual r (FP64 when only the solve runs in FP32).
+template <typename T, typename TR = T>
 struct OpIcUpper {
   const T* t;
-  const T* r;
+  const TR* r;
   PcgState* st;
   double* part;
   bool dn;
@@ -354,7 +355,7 @@ struct OpIcUpper {
     T t;
   };
   struct DPre {
-    T r;
+    TR r;
   };
   __device__ Pre pre(int i) const { return {t[i]}; }
   __device__ T rhs(int, const Pre& v) const { return v.t; }
@@ -371,10 +372,10 @@ struct OpIcUpper {
 
 // GS_std (k = 1) backward sweep: rhs_i = r_i - (A t)_i (GS.c:34-35),
 // y = (D+U)^-1 rhs, w = t + y (GS.c:40), reducing r'w.
-template <typename T>
+template <typename T, typename TR = T>
 struct OpGsUpper {
   const T* t;
-  const T* r;
+  const TR* r;
   const int* ia;
   const int* ja;
   const T* av;
@@ -390,15 +391,16 @@ struct OpGsUpper {
   __device__ bool active() const { return !dn; }
   __device__ void inactive_end() {}
   struct Pre {
-    T r;
+    TR r;
     int j0, j1;
   };
   struct DPre {
-    T t, r;
+    T t;
+    TR r;
   };
   __device__ Pre pre(int i) const { return {r[i], ia[i], ia[i + 1]}; }
   __device__ T rhs(int, const Pre& v) const {
-    T acc = v.r;
+    T acc = (T)v.r;
     for (int j = v.j0; j < v.j1; ++j) acc = fma_rn(-av[j], t[ja[j]], acc);
     return acc;
   }
@@ -417,6 +419,81 @@ struct OpGsUpper {
     rho_chunk_end(rho, st, part, c, nchunks, ticket, sm);
   }
 };
+
+// Lower solve of the split-precision recurrence: the FP64 residual r is the
+// right-hand side, rounded to the solve's type; the x / r update ran in the
+// FP64 update kernel before it.
+template <typename T, typename TR>
+struct OpSplitLower {
+  const TR* r;
+  T* sfill;
+  PcgState* st;
+  bool dn;
+  __device__ void begin() { dn = st->done != 0; }
+  __device__ bool active() const { return !dn; }
+  __device__ void inactive_end() {}
+  struct Pre {
+    TR r;
+  };
+  struct DPre {};
+  __device__ Pre pre(int i) const { return {r[i]}; }
+  __device__ T rhs(int, const Pre& v) const { return (T)v.r; }
+  __device__ DPre dpre(int) const { return {}; }
+  __device__ void done(int i, T, const DPre&) {
+    if (sfill) sfill[i] = sentinel<T>();
+  }
+  __device__ void prefetch(int r0, int r1, int part) const {
+    prefetch_rows_l2(r, r0, r1, part, kTriProdLanes);
+  }
+  __device__ void chunk_end(int, int nchunks, unsigned* ticket, double*) {
+    if (threadIdx.x == 0) chunk_finished(ticket, nchunks);
+  }
+};
+
+// ------------------------------------------------------------ spmv_pq (split)
+// Split precision: q = A w + beta q and p = w + beta p with w the FP32 output
+// of the preconditioner, A's FP32 values and FP32 products (A w), and p, q,
+// beta and p'q in FP64.  By linearity q = A p as in spmv_pq_kernel.
+__global__ void __launch_bounds__(kThreads)
+    spmv_pq_split_kernel(int n, int nb, const int* __restrict__ bundles, const int* __restrict__ ia,
+                         const int* __restrict__ ja, const float* __restrict__ a,
+                         const float* __restrict__ w, double* p, double* q, float* tfill,
+                         PcgState* st, double* part, cudaGraphConditionalHandle cond, int has_cond) {
+  __shared__ float stage[kThreads / 32][kBundleNnz];
+  __shared__ double sm[kThreads / 32];
+  if (has_cond && blockIdx.x == 0 && threadIdx.x == 0) {
+    const int g = ++st->spare_guard;
+    if (g > st->maxit + 8) set_cond(cond, true, false);
+  }
+  if (st->done) return;  // uniform across the grid
+  const bool first = st->iter == 0;
+  const double beta = first ? 0.0 : st->rho / st->rho_prev;
+  XPlain<float> xf{w};
+  struct Ep {
+    const float* w;
+    double *p, *q;
+    float* tf;
+    double beta;
+    bool first;
+    double pq;
+    __device__ float init(int) const { return 0.0f; }
+    __device__ void store(int i, float s) {
+      const double wi = (double)w[i];
+      const double pi = first ? wi : fma_rn(beta, p[i], wi);
+      const double qi = first ? (double)s : fma_rn(beta, q[i], (double)s);
+      p[i] = pi;
+      q[i] = qi;
+      pq = fma_rn(pi, qi, pq);
+      if (tf) tf[i] = sentinel<float>();
+    }
+  } ep{w, p, q, tfill, beta, first, 0.0};
+  const int wid = threadIdx.x >> 5;
+  for (int bb = blockIdx.x * (kThreads / 32) + wid; bb < nb; bb += gridDim.x * (kThreads / 32))
+    spmv_bundle<float, false>(bb, n, bundles, ia, ja, a, 1.0f, xf, ep, stage[wid]);
+  double acc[1] = {ep.pq};
+  if (reduce_last<1>(acc, part, gridDim.x, blockIdx.x, &st->tk[TK_PQ], sm) && threadIdx.x == 0)
+    st->pq = acc[0];
+}
 
 // ------------------------------------------------------------ true residual
 // ||b - A x|| and ||b|| in FP64 after the solve (cg.c:113-117).
@@ -449,24 +526,28 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------------ mixed precision helpers
-// Outer FP64 residual r = b - A x, its norm, cast to the FP32 inner rhs, and
-// the refinement stopping test against tol * ||b - A x0||.
+// Outer FP64 residual r = b - A x, its norm, stored as the inner recurrence's
+// residual (FP32 for the FP32 recurrence, FP64 for the split one; x32, when
+// given, is the FP32 correction to clear), and the refinement stopping test
+// against tol * ||b - A x0||.
+template <typename TR>
 __global__ void __launch_bounds__(kThreads)
     outer_resid_kernel(int n, int nb, const int* __restrict__ bundles, const int* __restrict__ ia,
                        const int* __restrict__ ja, const double* __restrict__ a,
-                       const double* __restrict__ b, const double* __restrict__ x, float* r32,
+                       const double* __restrict__ b, const double* __restrict__ x, TR* r32,
                        float* x32, PcgState* so, double* part, int first) {
   __shared__ double stage[kThreads / 32][kBundleNnz];
   __shared__ double sm[kThreads / 32];
   struct Ep {
     const double* b;
-    float *r32, *x32;
+    TR* r32;
+    float* x32;
     double a0;
     __device__ double init(int) const { return 0.0; }
     __device__ void store(int i, double v) {
       const double ri = b[i] - v;
-      r32[i] = (float)ri;
-      x32[i] = 0.0f;
+      r32[i] = (TR)ri;
+      if (x32) x32[i] = 0.0f;
       a0 += ri * ri;
     }
   } ep{b, r32, x32, 0.0};
@@ -500,15 +581,16 @@ __global__ void add_correction_kernel(int n, double* x, const float* __restrict_
 }
 
 // Residual replacement (mixed precision): after r was replaced by the FP64
-// true residual, the paused FP32 recurrence resumes -- p, q, rho_prev and the
-// iteration count are kept; the pause threshold moves to delta*||r||.
+// true residual, the paused recurrence resumes -- p, q, rho_prev and the
+// iteration count are kept; the pause threshold moves to delta*||r||, but not
+// below the solve's own target, so the last cycle stops at the tolerance.
 __global__ void resume_kernel(PcgState* st, const PcgState* so, double delta) {
   st->done = 0;
   st->flag = 1;
   st->status = GB_OK;
   st->spare_guard = 0;
   st->body_count = 0;
-  st->tolrel = delta * sqrt(so->rr);
+  st->tolrel = fmax(delta * sqrt(so->rr), so->tolrel);
 }
 
 // Jacobi / none after a residual replacement: w = D^-1 r, rho rolled.
@@ -595,18 +677,20 @@ static int launch_lower(gb_system sys, PcgState* st, int do_update, cudaGraphCon
   op.cond = cond;
   op.has_cond = has_cond;
   op.do_update = do_update;
-  return tri_launch<T, OpPcgLower<T>, false>(sys->L, tri_args<T>(sys->L, v.t, sys->err, true), op, sys->s);
+  const TriPlan& L = sizeof(T) == 8 ? sys->L : sys->L32;
+  return tri_launch<T, OpPcgLower<T>, false>(L, tri_args<T>(L, v.t, sys->err, true), op, sys->s);
 }
 
 template <typename T>
 static int launch_upper(gb_system sys, PcgState* st) {
   auto v = vecs<T>(sys);
+  const TriPlan& U = sizeof(T) == 8 ? sys->U : sys->U32;
   if (sys->prec == GB_PREC_ICHOL) {
     OpIcUpper<T> op{v.t, v.r, st, sys->part, false, 0.0};
-    return tri_launch<T, OpIcUpper<T>, false>(sys->U, tri_args<T>(sys->U, v.s, sys->err, true), op, sys->s);
+    return tri_launch<T, OpIcUpper<T>, false>(U, tri_args<T>(U, v.s, sys->err, true), op, sys->s);
   }
   OpGsUpper<T> op{v.t, v.r, sys->ia, sys->ja, mat_vals<T>(sys), v.w, st, sys->part, false, 0.0};
-  return tri_launch<T, OpGsUpper<T>, false>(sys->U, tri_args<T>(sys->U, v.s, sys->err, true), op, sys->s);
+  return tri_launch<T, OpGsUpper<T>, false>(U, tri_args<T>(U, v.s, sys->err, true), op, sys->s);
 }
 
 // w buffer the spmv_pq kernel gathers: ichol's w is the upper solve's output
@@ -649,6 +733,90 @@ int launch_prologue(gb_system sys, PcgState* st, int x_zero, const T* b) {
       return GB_NOT_SUPPORTED;
     }
   }
+  return GB_OK;
+}
+
+// ------------------------------------------------------------ split precision
+// FP64 recurrence (x, r, p, q, the scalars) around the FP32 operator and
+// preconditioner: the triangular solves run on the FMA-form FP32 records
+// with FP32 outputs t (lower) and s / w (upper).
+static int launch_lower_split(gb_system sys, PcgState* st) {
+  OpSplitLower<float, double> op{sys->v64.r, sys->v32.s, st, false};
+  return tri_launch<float, OpSplitLower<float, double>, false>(
+      sys->L32, tri_args<float>(sys->L32, sys->v32.t, sys->err, true), op, sys->s);
+}
+
+static int launch_upper_split(gb_system sys, PcgState* st) {
+  if (sys->prec == GB_PREC_ICHOL) {
+    OpIcUpper<float, double> op{sys->v32.t, sys->v64.r, st, sys->part, false, 0.0};
+    return tri_launch<float, OpIcUpper<float, double>, false>(
+        sys->U32, tri_args<float>(sys->U32, sys->v32.s, sys->err, true), op, sys->s);
+  }
+  OpGsUpper<float, double> op{sys->v32.t, sys->v64.r, sys->ia, sys->ja, sys->a32, sys->v32.w,
+                              st, sys->part, false, 0.0};
+  return tri_launch<float, OpGsUpper<float, double>, false>(
+      sys->U32, tri_args<float>(sys->U32, sys->v32.s, sys->err, true), op, sys->s);
+}
+
+static int grid_split(int nb) {
+  return wave_grid(spmv_pq_split_kernel, kThreads, ceil_div(nb, kThreads / 32));
+}
+
+// w = M^-1 r for the current FP64 r (the lower solve's output is pre-filled
+// with the sentinel first); the upper solve rolls rho.
+static int apply_prec_split(gb_system sys, PcgState* st) {
+  GB_TRY(fill_sentinel_dev(sys->n, sys->v32.t, sys->s));
+  GB_TRY(launch_lower_split(sys, st));
+  return launch_upper_split(sys, st);
+}
+
+int launch_prologue_split(gb_system sys, PcgState* st, const double* b) {
+  if (!prec_fused_tri(sys->prec, sys->k)) return GB_NOT_SUPPORTED;
+  const int nb = sys->plan.nbundles;
+  resid_kernel<double, WK_PREC><<<grid_for_bundles<double>(nb), kThreads, 0, sys->s>>>(
+      sys->n, nb, sys->plan.bundles, sys->ia, sys->ja, sys->a, b, sys->v64.x, 0, sys->v64.r,
+      nullptr, nullptr, nullptr, st, sys->part, sys->hist);
+  GB_CUDA_TRY(cudaGetLastError());
+  return apply_prec_split(sys, st);
+}
+
+int launch_body_split(gb_system sys, PcgState* st, cudaGraphConditionalHandle cond, int has_cond) {
+  if (!prec_fused_tri(sys->prec, sys->k)) return GB_NOT_SUPPORTED;
+  auto& v = sys->v64;
+  const int nb = sys->plan.nbundles;
+  const float* w = sys->prec == GB_PREC_ICHOL ? sys->v32.s : sys->v32.w;
+  spmv_pq_split_kernel<<<grid_split(nb), kThreads, 0, sys->s>>>(
+      sys->n, nb, sys->plan.bundles, sys->ia, sys->ja, sys->a32, w, v.p0, v.q, sys->v32.t, st,
+      sys->part, cond, has_cond);
+  GB_CUDA_TRY(cudaGetLastError());
+  const double n = sys->n, nz = sys->nnz;
+  if (g_prof) prof_mark(sys->s, "spmv_pq_split", nz * 8.0 + (n + 1) * 4.0 + n * (4 + 4 * 8 + 4));
+  update_kernel<double, WK_PREC><<<grid_ew(sys->n), kThreads, 0, sys->s>>>(
+      sys->n, v.x, v.r, nullptr, v.p0, v.q, nullptr, st, sys->part, sys->hist, cond, has_cond);
+  GB_CUDA_TRY(cudaGetLastError());
+  if (g_prof) prof_mark(sys->s, "update", 6 * n * 8.0);
+  GB_TRY(launch_lower_split(sys, st));
+  if (g_prof) prof_mark(sys->s, "lower_solve_split", sys->L32.ndeps * 8.0 + n * 8.0 + n * 8.0 + n * 8.0);
+  GB_TRY(launch_upper_split(sys, st));
+  if (g_prof)
+    prof_mark(sys->s, sys->prec == GB_PREC_ICHOL ? "upper_solve_split" : "gs_upper_solve_split",
+              sys->U32.ndeps * 8.0 + n * 8.0 + n * 4.0 + n * 8.0 + n * 4.0 +
+                  (sys->prec == GB_PREC_ICHOL ? 0.0 : nz * 8.0 + (n + 1) * 4.0 + n * 8.0));
+  return GB_OK;
+}
+
+int launch_resume_split(gb_system sys, PcgState* st, double delta) {
+  resume_kernel<<<1, 1, 0, sys->s>>>(st, sys->st_out, delta);
+  GB_CUDA_TRY(cudaGetLastError());
+  return apply_prec_split(sys, st);
+}
+
+int launch_outer_resid64(gb_system sys, const double* b, const double* x, int first) {
+  const int nb = sys->plan.nbundles;
+  outer_resid_kernel<double><<<grid_for_bundles<double>(nb), kThreads, 0, sys->s>>>(
+      sys->n, nb, sys->plan.bundles, sys->ia, sys->ja, sys->a, b, x, sys->v64.r, nullptr,
+      sys->st_out, sys->part, first);
+  GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
 
@@ -737,7 +905,7 @@ int launch_true_resid(gb_system sys, const double* b, const double* x, double* o
 
 int launch_outer_resid(gb_system sys, const double* b, const double* x, int first) {
   const int nb = sys->plan.nbundles;
-  outer_resid_kernel<<<grid_for_bundles<double>(nb), kThreads, 0, sys->s>>>(
+  outer_resid_kernel<float><<<grid_for_bundles<double>(nb), kThreads, 0, sys->s>>>(
       sys->n, nb, sys->plan.bundles, sys->ia, sys->ja, sys->a, b, x, sys->v32.r, sys->v32.x,
       sys->st_out, sys->part, first);
   GB_CUDA_TRY(cudaGetLastError());
@@ -750,7 +918,10 @@ int launch_resume(gb_system sys, PcgState* st, double delta) {
   GB_CUDA_TRY(cudaGetLastError());
   auto v = vecs<T>(sys);
   if (prec_fused_tri(sys->prec, sys->k)) {
-    // w = M^-1 r for the replaced r; the upper solve rolls rho
+    // w = M^-1 r for the replaced r; the upper solve rolls rho.  The lower
+    // solve's output still holds the last solve's values: refill it with the
+    // sentinel, or later tiles would read them as finished.
+    GB_TRY(fill_sentinel_dev(sys->n, v.t, sys->s));
     GB_TRY(launch_lower<T>(sys, st, 0, 0, 0));
     return launch_upper<T>(sys, st);
   }
@@ -778,7 +949,9 @@ int part_len_needed(gb_system sys) {
   int m = std::max(std::max(grid_for_bundles<double>(sys->plan.nbundles),
                             grid_for_bundles<float>(sys->plan.nbundles)),
                    reduction_grid());
-  if (sys->tri) m = std::max(m, std::max(sys->L.ntiles, sys->U.ntiles));
+  m = std::max(m, grid_split(sys->plan.nbundles));
+  if (sys->tri) m = std::max(m, std::max(std::max(sys->L.ntiles, sys->U.ntiles),
+                                         std::max(sys->L32.ntiles, sys->U32.ntiles)));
   return 2 * m + 64;
 }
 

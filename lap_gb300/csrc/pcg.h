@@ -16,6 +16,15 @@ int launch_prologue(gb_system sys, PcgState* st, int x_zero, const T* b);
 template <typename T>
 int launch_body(gb_system sys, PcgState* st, cudaGraphConditionalHandle cond, int has_cond);
 
+// Split precision (ichol, GS_std with k = 1): FP64 recurrence, FP32 SpMV
+// values and FP32 triangular solves.  The resume replaces nothing itself:
+// launch_outer_resid64 writes the FP64 true residual into the recurrence's
+// r first.
+int launch_prologue_split(gb_system sys, PcgState* st, const double* b);
+int launch_body_split(gb_system sys, PcgState* st, cudaGraphConditionalHandle cond, int has_cond);
+int launch_resume_split(gb_system sys, PcgState* st, double delta);
+int launch_outer_resid64(gb_system sys, const double* b, const double* x, int first);
+
 int launch_true_resid(gb_system sys, const double* b, const double* x, double* out2);
 int launch_outer_resid(gb_system sys, const double* b, const double* x, int first);
 int launch_add_correction(gb_system sys, double* x);

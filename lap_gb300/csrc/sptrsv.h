@@ -30,17 +30,25 @@ int deps_ichol(int n, const int* ia, const int* ja, const std::vector<int>& tpos
                TriDeps* d);
 
 // tile_rows <= 0: one tile per SM for large matrices, 1024..16384 rows.
+// Tiles of more than kTriMaxTileRows64 rows (up to kTriMaxTileRows32) fit
+// shared memory only as FP32 and may be solved in FP32 only.
+constexpr int kTriMaxTileRows64 = 16384;
+constexpr int kTriMaxTileRows32 = 32768;
 int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows = 0);
 int tri_default_tile_rows(int n);
+// Tile rows of the FP32-only plans: twice the FP64 default (32768 at most).
+int tri_default_tile_rows32(int n);
 // Resident CTAs per SM of the tiled solves (default 1, limited by shared
 // memory anyway); GBLAP_TRI_BLOCKS_PER_SM overrides it (1..8).
 int tri_grid(int ntiles);
 int tri_blocks_per_sm();
 void tri_set_blocks_per_sm(int bps);
 void tri_plan_free(TriPlan* plan);
-// Writes the record values from value arrays: the exact FP64 records and,
-// when for_pcg, the FMA-form FP64 and FP32 records the PCG solves read.
-int tri_plan_fill(TriPlan* plan, const double* ent_src, const double* diag_src, bool for_pcg,
+// Writes the record values from value arrays: always the exact FP64 records;
+// kFillFma64 adds the FMA-form FP64 copy, kFillFma32 the FMA-form FP32
+// records (what the PCG's FP64 / FP32 solves read).
+enum { kFillExact = 0, kFillFma64 = 1, kFillFma32 = 2 };
+int tri_plan_fill(TriPlan* plan, const double* ent_src, const double* diag_src, int mode,
                   cudaStream_t s);
 
 // y = T^{-1} x with the plan's values, rounded as the reference rounds.  y

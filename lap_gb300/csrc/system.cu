@@ -50,7 +50,7 @@ extern "C" void gb_pcg_opts_default(gb_pcg_opts* o) {
   o->tol = 1e-8;
   o->maxit = 10000;
   o->precision = 0;
-  o->inner_tol = 1e-4;
+  o->inner_tol = 0.0;  // the mode's default
   o->max_outer = 50;
   o->use_graph = 1;
   o->verbose = 0;
@@ -136,6 +136,8 @@ static void system_free(gb_system s) {
   spmv_plan_free(&s->plan);
   tri_plan_free(&s->L);
   tri_plan_free(&s->U);
+  tri_plan_free(&s->L32);
+  tri_plan_free(&s->U32);
   void* ptrs[] = {s->dpos, s->tpos, s->diag, s->d_r, s->d_r32, s->a32, s->fac, s->fac_done,
                   s->zero_pivot, s->fac_ticket, s->lia, s->lja, s->uia, s->uja, s->la, s->ua,
                   s->v64.x, s->v64.r, s->v64.w, s->v64.p0, s->v64.p1, s->v64.q, s->v64.t,
@@ -180,13 +182,17 @@ static int setup_values(gb_system s) {
   GB_TRY(cast_f64_to_f32(n, s->d_r, s->d_r32, s->s));
   GB_TRY(cast_f64_to_f32(s->nnz, s->a, s->a32, s->s));
   if (s->prec == GB_PREC_GS_STD) {
-    GB_TRY(tri_plan_fill(&s->L, s->a, s->a, true, s->s));
-    GB_TRY(tri_plan_fill(&s->U, s->a, s->a, true, s->s));
+    GB_TRY(tri_plan_fill(&s->L, s->a, s->a, kFillFma64, s->s));
+    GB_TRY(tri_plan_fill(&s->U, s->a, s->a, kFillFma64, s->s));
+    GB_TRY(tri_plan_fill(&s->L32, s->a, s->a, kFillFma32, s->s));
+    GB_TRY(tri_plan_fill(&s->U32, s->a, s->a, kFillFma32, s->s));
   } else if (s->prec == GB_PREC_ICHOL) {
     GB_TRY(ichol_factor_dev(n, s->ia, s->ja, s->a, s->dpos, s->tpos, &s->L, s->fac, s->fac_done,
                             s->fac_ticket, s->zero_pivot, s->err, s->s));
-    GB_TRY(tri_plan_fill(&s->L, s->fac, s->fac, true, s->s));
-    GB_TRY(tri_plan_fill(&s->U, s->fac, s->fac, true, s->s));
+    GB_TRY(tri_plan_fill(&s->L, s->fac, s->fac, kFillFma64, s->s));
+    GB_TRY(tri_plan_fill(&s->U, s->fac, s->fac, kFillFma64, s->s));
+    GB_TRY(tri_plan_fill(&s->L32, s->fac, s->fac, kFillFma32, s->s));
+    GB_TRY(tri_plan_fill(&s->U32, s->fac, s->fac, kFillFma32, s->s));
   } else if (s->prec == GB_PREC_IT_JACOBI || s->prec == GB_PREC_GS_IT || s->prec == GB_PREC_GS_IT2) {
     GB_TRY(gather_values(s->lnnz, s->lmap_cpu, s->a, s->la, nullptr, s->s));
     GB_TRY(gather_values(s->unnz, s->umap_cpu, s->a, s->ua, nullptr, s->s));
@@ -266,6 +272,12 @@ extern "C" int gb_system_create(int n, int nnz, const int* ia, const int* ja, co
     }
     CK(tri_plan_build(dl, &s->L));
     CK(tri_plan_build(du, &s->U));
+    // IC(0)'s rows are cheap to start, so FP32 tiles twice as tall (half the
+    // tile-boundary crossings) pay; GS_std's backward sweep gathers a row of
+    // A per row and needs the parallelism of the FP64 tiling
+    const int t32 = prec == GB_PREC_ICHOL ? tri_default_tile_rows32(n) : tri_default_tile_rows(n);
+    CK(tri_plan_build(dl, &s->L32, t32));
+    CK(tri_plan_build(du, &s->U32, t32));
   }
   if (prec == GB_PREC_IT_JACOBI || prec == GB_PREC_GS_IT || prec == GB_PREC_GS_IT2) {
     std::vector<int> lp(n + 1, 0), up(n + 1, 0), lj, uj, lm, um;
@@ -340,8 +352,9 @@ extern "C" int gb_system_info(gb_system s, int* lower_levels, int* upper_levels,
 // ------------------------------------------------------------ solve loop
 // Builds (once) a graph holding only a while node whose body is one PCG
 // iteration; the body's checking kernel sets the condition.
-template <typename T>
-static int get_loop_graph(gb_system s, int idx, LoopGraph** out) {
+using BodyFn = int (*)(gb_system, PcgState*, cudaGraphConditionalHandle, int);
+
+static int get_loop_graph(gb_system s, int idx, BodyFn body_fn, LoopGraph** out) {
   LoopGraph* lg = &s->loop[idx];
   const int key = s->hist_cap;
   if (lg->exec && s->loop_key[idx] == key) {
@@ -368,7 +381,7 @@ static int get_loop_graph(gb_system s, int idx, LoopGraph** out) {
   GB_CUDA_TRY(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   GB_CUDA_TRY(cudaStreamBeginCaptureToGraph(s->s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  const int rc = launch_body<T>(s, s->st, h, 1);
+  const int rc = body_fn(s, s->st, h, 1);
   cudaGraph_t captured = nullptr;
   const cudaError_t e = cudaStreamEndCapture(s->s, &captured);
   if (rc != GB_OK || e != cudaSuccess) {
@@ -384,29 +397,35 @@ static int get_loop_graph(gb_system s, int idx, LoopGraph** out) {
 }
 
 // Runs one PCG recurrence on the system stream: prologue, then the loop.
-template <typename T>
-static int run_loop(gb_system s, int maxit, int use_graph);
+static int run_loop(gb_system s, int idx, BodyFn body_fn, int maxit, int use_graph);
 
 template <typename T>
 static int run_recurrence(gb_system s, double tol, int maxit, int x_zero, const T* b, int use_graph) {
   init_state_host(s->st_host, tol, maxit, s->hist_cap);
   GB_CUDA_TRY(cudaMemcpyAsync(s->st, s->st_host, sizeof(PcgState), cudaMemcpyHostToDevice, s->s));
   GB_TRY(launch_prologue<T>(s, s->st, x_zero, b));
-  return run_loop<T>(s, maxit, use_graph);
+  return run_loop(s, sizeof(T) == 8 ? 0 : 1, &launch_body<T>, maxit, use_graph);
+}
+
+// Split precision: FP64 recurrence from x (not zeroed), FP32 operator and
+// preconditioner.
+static int run_recurrence_split(gb_system s, double tol, int maxit, const double* b, int use_graph) {
+  init_state_host(s->st_host, tol, maxit, s->hist_cap);
+  GB_CUDA_TRY(cudaMemcpyAsync(s->st, s->st_host, sizeof(PcgState), cudaMemcpyHostToDevice, s->s));
+  GB_TRY(launch_prologue_split(s, s->st, b));
+  return run_loop(s, 2, &launch_body_split, maxit, use_graph);
 }
 
 // Runs (or resumes) the iteration loop until the recurrence's done flag.
-template <typename T>
-static int run_loop(gb_system s, int maxit, int use_graph) {
-  const int idx = sizeof(T) == 8 ? 0 : 1;
+static int run_loop(gb_system s, int idx, BodyFn body_fn, int maxit, int use_graph) {
   if (use_graph) {
     LoopGraph* lg = nullptr;
-    GB_TRY(get_loop_graph<T>(s, idx, &lg));
+    GB_TRY(get_loop_graph(s, idx, body_fn, &lg));
     GB_CUDA_TRY(cudaGraphLaunch(lg->exec, s->s));
   } else {
     // eager: a status read every 16 iterations
     for (int it = 0; it <= maxit + 1; it += 16) {
-      for (int j = 0; j < 16; ++j) GB_TRY(launch_body<T>(s, s->st, 0, 0));
+      for (int j = 0; j < 16; ++j) GB_TRY(body_fn(s, s->st, 0, 0));
       GB_CUDA_TRY(cudaMemcpyAsync(s->st_host, s->st, sizeof(PcgState), cudaMemcpyDeviceToHost, s->s));
       GB_CUDA_TRY(cudaStreamSynchronize(s->s));
       if (s->st_host->done) break;
@@ -429,6 +448,9 @@ static int solve_internal(gb_system s, const gb_pcg_opts* o, gb_pcg_result* res,
   gb_pcg_result r;
   memset(&r, 0, sizeof r);
   PcgState* hs = s->st_host;
+  // residual reduction between replacements: FP32 Krylov vectors (1) drift
+  // slowly, the FP32 operator under FP64 vectors (2) is best replaced often
+  const double itol = o->inner_tol > 0.0 ? o->inner_tol : (o->precision == 2 ? 1e-2 : 1e-4);
   if (o->precision == 0) {
     GB_TRY(run_recurrence<double>(s, o->tol, o->maxit, 0, s->b_int, o->use_graph));
     GB_TRY(launch_true_resid(s, s->b_int, s->v64.x, s->scratch));
@@ -442,7 +464,58 @@ static int solve_internal(gb_system s, const gb_pcg_opts* o, gb_pcg_result* res,
       const int cnt = std::min(hist_len, std::min(hs->iter + 1, s->hist_cap));
       GB_CUDA_TRY(cudaMemcpy(hist_host, s->hist, sizeof(double) * cnt, cudaMemcpyDeviceToHost));
     }
-  } else {
+  } else if (o->precision == 2) {
+    if (!prec_fused_tri(s->prec, s->k)) return GB_NOT_SUPPORTED;
+    PcgState* ho = s->st_host + 1;
+    init_state_host(ho, o->tol, o->maxit, 0);
+    GB_CUDA_TRY(cudaMemcpyAsync(s->st_out, ho, sizeof(PcgState), cudaMemcpyHostToDevice, s->s));
+    // FP64 recurrence around the FP32 operator and preconditioner.  The
+    // recursive residual drifts from b - A x by the FP32 rounding of A w that
+    // q accumulates, so the recurrence pauses whenever its residual has
+    // dropped by inner_tol since the last replacement; r is then replaced by
+    // the FP64 true residual and the recurrence resumes with x, p, q and rho
+    // intact.  Convergence is judged on the FP64 residual only.
+    int total = 0, outer = 0, flag = 1, status = GB_MAXIT;
+    GB_TRY(launch_outer_resid64(s, s->b_int, s->v64.x, 1));
+    GB_TRY(read_state(s, ho, s->st_out));
+    double last_res = std::sqrt(ho->rr);
+    if (hist_host && hist_len > 0) hist_host[0] = last_res;
+    if (ho->done) {
+      flag = ho->flag;
+      status = ho->status;
+    } else {
+      GB_TRY(run_recurrence_split(s, std::max(itol, o->tol), o->maxit, s->b_int, o->use_graph));
+      for (;;) {
+        GB_TRY(read_state(s, hs, s->st));
+        total = hs->iter;
+        if (hs->status == GB_BREAKDOWN) {
+          flag = 2;
+          status = GB_BREAKDOWN;
+          break;
+        }
+        GB_TRY(launch_outer_resid64(s, s->b_int, s->v64.x, 0));
+        GB_TRY(read_state(s, ho, s->st_out));
+        ++outer;
+        last_res = std::sqrt(ho->rr);
+        if (hist_host && outer < hist_len) hist_host[outer] = last_res;
+        if (ho->done) {
+          flag = ho->flag;
+          status = ho->status;
+          break;
+        }
+        if (hs->flag == 1 || outer >= o->max_outer) break;  // out of iterations
+        GB_TRY(launch_resume_split(s, s->st, itol));
+        GB_TRY(run_loop(s, 2, &launch_body_split, o->maxit, o->use_graph));
+      }
+    }
+    r.iters = total;
+    r.outer = outer;
+    r.flag = flag;
+    r.status = status;
+    r.res0 = ho->res0;
+    r.res = last_res;
+    GB_TRY(launch_true_resid(s, s->b_int, s->v64.x, s->scratch));
+  } else if (o->precision == 1) {
     if (!(s->prec == GB_PREC_LINE_JACOBI || s->prec == GB_PREC_NONE || prec_fused_tri(s->prec, s->k)))
       return GB_NOT_SUPPORTED;
     PcgState* ho = s->st_host + 1;
@@ -465,7 +538,7 @@ static int solve_internal(gb_system s, const gb_pcg_opts* o, gb_pcg_result* res,
       flag = ho->flag;
       status = ho->status;
     } else {
-      GB_TRY(run_recurrence<float>(s, o->inner_tol, o->maxit, 1, s->v32.r, o->use_graph));
+      GB_TRY(run_recurrence<float>(s, std::max(itol, o->tol), o->maxit, 1, s->v32.r, o->use_graph));
       for (;;) {
         GB_TRY(read_state(s, hs, s->st));
         total = hs->iter;
@@ -486,8 +559,8 @@ static int solve_internal(gb_system s, const gb_pcg_opts* o, gb_pcg_result* res,
           break;
         }
         if (hs->flag == 1 || outer >= o->max_outer) break;  // out of iterations
-        GB_TRY(launch_resume<float>(s, s->st, o->inner_tol));
-        GB_TRY(run_loop<float>(s, o->maxit, o->use_graph));
+        GB_TRY(launch_resume<float>(s, s->st, itol));
+        GB_TRY(run_loop(s, 1, &launch_body<float>, o->maxit, o->use_graph));
       }
     }
     r.iters = total;
@@ -497,6 +570,8 @@ static int solve_internal(gb_system s, const gb_pcg_opts* o, gb_pcg_result* res,
     r.res0 = ho->res0;
     r.res = last_res;
     GB_TRY(launch_true_resid(s, s->b_int, s->v64.x, s->scratch));
+  } else {
+    return GB_BAD_INPUT;
   }
   double tr[2] = {0.0, 0.0};
   GB_CUDA_TRY(cudaMemcpyAsync(tr, s->scratch, sizeof tr, cudaMemcpyDeviceToHost, s->s));

@@ -47,9 +47,11 @@ struct gb_system_s {
   float* d_r32 = nullptr;
   float* a32 = nullptr;
 
-  // triangular schedules (GS_std, ichol)
+  // triangular schedules (GS_std, ichol): L, U for the FP64 solves (exact and
+  // FMA form); L32, U32 for the FP32 solves, with tiles twice as tall
   bool tri = false;
   gb::TriPlan L, U;
+  gb::TriPlan L32, U32;
   double* fac = nullptr;  // IC(0) factor on A's pattern
   int* fac_done = nullptr;
   int* zero_pivot = nullptr;
@@ -83,8 +85,8 @@ struct gb_system_s {
   int* err = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
-  gb::LoopGraph loop[2];  // [precision]
-  int loop_key[2] = {-1, -1};
+  gb::LoopGraph loop[3];  // [precision]
+  int loop_key[3] = {-1, -1, -1};
 };
 
 namespace gb {

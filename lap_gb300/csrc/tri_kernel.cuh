@@ -50,14 +50,22 @@
 
 namespace gb {
 
-constexpr int kTriConsumers = 8;                       // consumer warps
-constexpr int kTriThreads = (kTriConsumers + 1) * 32;  // + one producer warp
+// Consumer warps per CTA.  FP64 solves use 8: GB300 issues one FP64 lane op
+// per two cycles per SM sub-partition, so more warps only queue their FP64
+// work in front of the dependency chain.  FP32 solves have no such limit and
+// use 16, which keeps more records' loads in flight.
+template <typename T>
+struct TriCons {
+  static constexpr int n = sizeof(T) == 8 ? 8 : 16;
+  static constexpr int threads = (n + 1) * 32;  // + one producer warp
+};
 constexpr int kTriSlots = 40;                          // ring depth (records in flight)
 constexpr int kTriSlotBytes = 2048;                    // max record size
 constexpr int kTriL2Ahead = 32;                        // records prefetched into L2 ahead of the ring
 constexpr int kTriProdLanes = 8;                       // producer lanes issuing copies in parallel
 static_assert(kTriSlots % kTriProdLanes == 0, "a slot is always refilled by the same producer lane");
 constexpr int kTriRecTable = 1024;                     // records of a tile cached in smem
+constexpr int kTriMaxDynSmem = 212 * 1024;             // ring + the largest tile (FP32 x 32768 rows)
 constexpr int kTriRecRows = 32;                        // rows per record (one per lane)
 constexpr int kRecLong = 2;                            // record flag: one row, warp-reduced
 
@@ -336,7 +344,9 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
 }
 
 template <typename T, typename OP, bool EXACT>
-__global__ void __launch_bounds__(kTriThreads, 1) tri_tile_kernel(TriArgs<T> A, OP op) {
+__global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArgs<T> A, OP op) {
+  constexpr int kTriConsumers = TriCons<T>::n;
+  constexpr int kTriThreads = TriCons<T>::threads;
   extern __shared__ __align__(128) unsigned char tri_smem[];
   unsigned char* ring = tri_smem;                                     // kTriSlots x kTriSlotBytes
   T* sy = reinterpret_cast<T*>(tri_smem + kTriSlots * kTriSlotBytes);  // tile solution
@@ -467,15 +477,16 @@ template <typename T, typename OP, bool EXACT>
 int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   if (p.ntiles <= 0) return GB_OK;
   const size_t smem = (size_t)kTriSlots * kTriSlotBytes + (size_t)p.tile_rows * sizeof(T);
+  if (smem > (size_t)kTriMaxDynSmem) return GB_NOT_SUPPORTED;  // an FP32-only plan in FP64
   static bool attr_set = false;  // one per instantiation
   if (!attr_set) {
     GB_CUDA_TRY(cudaFuncSetAttribute(tri_tile_kernel<T, OP, EXACT>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 212 * 1024));
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kTriMaxDynSmem));
     attr_set = true;
   }
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tri_tile_kernel<T, OP, EXACT>,
-                                                    kTriThreads, smem) != cudaSuccess ||
+                                                    TriCons<T>::threads, smem) != cudaSuccess ||
       per_sm < 1) {
     cudaGetLastError();
     per_sm = 1;
@@ -483,7 +494,7 @@ int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   per_sm = per_sm < tri_blocks_per_sm() ? per_sm : tri_blocks_per_sm();
   const long long cap = (long long)device_sm_count() * per_sm;
   const int grid = (int)(p.ntiles < cap ? p.ntiles : cap);
-  tri_tile_kernel<T, OP, EXACT><<<grid, kTriThreads, smem, s>>>(A, op);
+  tri_tile_kernel<T, OP, EXACT><<<grid, TriCons<T>::threads, smem, s>>>(A, op);
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }

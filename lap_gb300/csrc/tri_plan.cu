@@ -23,7 +23,7 @@ int tri_default_tile_rows(int n) {
   // GBLAP_TRI_TILE_ROWS overrides (32..16384; the autotuner's knob)
   if (const char* e = getenv("GBLAP_TRI_TILE_ROWS")) {
     const int v = atoi(e);
-    if (v >= 32 && v <= 16384) return v;
+    if (v >= 32 && v <= kTriMaxTileRows64) return v;
   }
   // one tile per SM when the matrix is large; at least 1024 rows, at most
   // 16384 (128 KB of FP64 shared memory beside the 64 KB record ring)
@@ -141,7 +141,7 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
   const int n = d.n;
   const bool lower = d.lower;
   if (tile_rows <= 0) tile_rows = tri_default_tile_rows(n);
-  tile_rows = std::max(32, std::min(tile_rows, 16384));
+  tile_rows = std::max(32, std::min(tile_rows, kTriMaxTileRows32));
   auto deps_of = [&](int r) { return d.row_ptr[r + 1] - d.row_ptr[r]; };
 
   // global levels: the IC(0) factorization order and a diagnostic
@@ -302,8 +302,9 @@ __global__ void fill_records_kernel(int nval, const long long* __restrict__ vdst
 
 // FMA form: every short record's entry values times the reciprocal of their
 // row's diagonal, computed in FP64 from the exact records and written to the
-// FP64 copy (which already holds the rest of the record) and rounded once to
-// the FP32 records.  One warp per record, one lane per row.
+// FP64 copy (which already holds the rest of the record) and / or rounded
+// once to the FP32 records (either may be null).  One warp per record, one
+// lane per row.
 __global__ void scale_records_kernel(int nrec, const long long* __restrict__ off64,
                                      const unsigned char* __restrict__ buf64,
                                      const long long* __restrict__ off32, unsigned char* buf32,
@@ -319,17 +320,28 @@ __global__ void scale_records_kernel(int nrec, const long long* __restrict__ off
     const size_t vals32 = sizeof(RecHdr) + (size_t)R4 * (4 + 4 + 4) + (size_t)h.len * R4 * 4;
     const double dinv = reinterpret_cast<const double*>(r + sizeof(RecHdr) + (size_t)R4 * 12)[lane];
     const double* v = reinterpret_cast<const double*>(r + vals64);
-    double* vs = reinterpret_cast<double*>(buf64s + off64[rec] + vals64);
-    float* v32 = reinterpret_cast<float*>(buf32 + off32[rec] + vals32);
+    double* vs = buf64s ? reinterpret_cast<double*>(buf64s + off64[rec] + vals64) : nullptr;
+    float* v32 = buf32 ? reinterpret_cast<float*>(buf32 + off32[rec] + vals32) : nullptr;
     for (int k = 0; k < h.len; ++k) {
       const double x = v[k * R4 + lane] * dinv;
-      vs[k * R4 + lane] = x;
-      v32[k * R4 + lane] = (float)x;
+      if (vs) vs[k * R4 + lane] = x;
+      if (v32) v32[k * R4 + lane] = (float)x;
     }
   }
 }
 
-int tri_plan_fill(TriPlan* p, const double* ent_src, const double* diag_src, bool for_pcg,
+int tri_default_tile_rows32(int n) {
+  // GBLAP_TRI_TILE_ROWS32 overrides (32..32768)
+  if (const char* e = getenv("GBLAP_TRI_TILE_ROWS32")) {
+    const int v = atoi(e);
+    if (v >= 32 && v <= kTriMaxTileRows32) return v;
+  }
+  // FP32 values take half the shared memory: twice the FP64 tile, so a
+  // dependency chain crosses half as many tile boundaries
+  return std::min(kTriMaxTileRows32, 2 * tri_default_tile_rows(n));
+}
+
+int tri_plan_fill(TriPlan* p, const double* ent_src, const double* diag_src, int mode,
                   cudaStream_t s) {
   const int g = std::max(1, std::min(device_sm_count() * 8, ceil_div(std::max(p->nval, p->ndiag), 256)));
   fill_records_kernel<double><<<g, 256, 0, s>>>(p->nval, p->r64.vdst, p->vsrc, ent_src, p->ndiag,
@@ -337,21 +349,26 @@ int tri_plan_fill(TriPlan* p, const double* ent_src, const double* diag_src, boo
                                                 p->nlong, p->long_src, (double*)p->r64.buf,
                                                 (double*)p->r64.long_val);
   GB_CUDA_TRY(cudaGetLastError());
-  if (for_pcg) {
+  if (mode == kFillFma32) {
     fill_records_kernel<float><<<g, 256, 0, s>>>(p->nval, p->r32.vdst, p->vsrc, ent_src, p->ndiag,
                                                  p->r32.ddst, p->r32.idst, p->dsrc, diag_src,
                                                  p->nlong, p->long_src, (float*)p->r32.buf,
                                                  (float*)p->r32.long_val);
     GB_CUDA_TRY(cudaGetLastError());
+    p->have32 = true;
+  }
+  if (mode == kFillFma64) {
     if (!p->buf64s) GB_CUDA_TRY(cudaMalloc(&p->buf64s, (size_t)p->r64.bytes));
     GB_CUDA_TRY(cudaMemcpyAsync(p->buf64s, p->r64.buf, (size_t)p->r64.bytes, cudaMemcpyDeviceToDevice, s));
+  }
+  if (mode != kFillExact) {
     if (p->nrec > 0) {
       const int gs = std::max(1, std::min(device_sm_count() * 8, ceil_div(p->nrec, 8)));
-      scale_records_kernel<<<gs, 256, 0, s>>>(p->nrec, p->r64.off, p->r64.buf, p->r32.off, p->r32.buf,
-                                              p->buf64s);
+      scale_records_kernel<<<gs, 256, 0, s>>>(p->nrec, p->r64.off, p->r64.buf, p->r32.off,
+                                              mode == kFillFma32 ? p->r32.buf : nullptr,
+                                              mode == kFillFma64 ? p->buf64s : nullptr);
       GB_CUDA_TRY(cudaGetLastError());
     }
-    p->have32 = true;
   }
   return GB_OK;
 }

@@ -89,6 +89,59 @@ def test_mixed_precision_error_vs_fp64_oracle(prec):
     sysm.close()
 
 
+@pytest.mark.parametrize("prec", ["ichol", "GS_std"])
+def test_split_precision_error_vs_fp64_oracle(prec):
+    """precision=2: FP64 recurrence around the FP32 SpMV and FP32 triangular
+    solves; at tol 1e-10 the error against the FP64 oracle stays at the FP64
+    level (more iterations than FP64: each replacement cycle is limited by the
+    FP32 operator's rounding)."""
+    A, b = gen.grid3d_lognormal(20, seed=1002)
+    ref = oracle.solve(A.n, A.ia, A.ja, A.a, b, prec, 1e-13, 20000)
+    sysm = gb.System.from_csr(A, prec)
+    x, r = sysm.solve(dev(b), tol=1e-10, maxit=20000, precision=2)
+    assert r["flag"] == 0 and r["status"] == 0 and r["outer"] >= 1
+    assert r["rel_true_res"] < 1e-10 * 1.01
+    err = np.linalg.norm(x.cpu().numpy() - ref["x"]) / np.linalg.norm(ref["x"])
+    assert err < 1e-8, err
+    sysm.close()
+
+
+@pytest.mark.parametrize("prec", ["ichol", "GS_std"])
+def test_split_precision_iterations_at_1e8(prec):
+    """At tol 1e-8 the split recurrence needs as many iterations as the FP64
+    PCG, within the +-2% asked of GS / IC0 (64^3; very small systems, where a
+    last replacement cycle weighs more, may need a few more)."""
+    A, b = gen.grid3d_lognormal(64, seed=1002)
+    sysm = gb.System.from_csr(A, prec)
+    _, r = sysm.solve(dev(b), tol=1e-8, maxit=20000, precision=2)
+    _, r64 = sysm.solve(dev(b), tol=1e-8, maxit=20000, precision=0)
+    assert r["flag"] == 0 and r["rel_true_res"] < 1e-8 * 1.01
+    assert iters_ok(r["iters"], r64["iters"], prec), (r["iters"], r64["iters"])
+    sysm.close()
+
+
+@pytest.mark.parametrize("prec", ["ichol", "GS_std"])
+def test_split_precision_graph_eager_and_x0(prec):
+    A, b = gen.grid2d_unit(48, seed=11)
+    sysm = gb.System.from_csr(A, prec)
+    x1, r1 = sysm.solve(dev(b), tol=1e-9, maxit=3000, precision=2, use_graph=True)
+    x2, r2 = sysm.solve(dev(b), tol=1e-9, maxit=3000, precision=2, use_graph=False)
+    assert r1["iters"] == r2["iters"] and r1["flag"] == r2["flag"] == 0
+    assert torch.equal(x1, x2)
+    # a nonzero x0 (tolerance relative to ||b - A x0||, as cg.c)
+    x4, r4 = sysm.solve(dev(b), x=x1 * 0.5, tol=1e-9, maxit=3000, precision=2)
+    assert r4["flag"] == 0 and r4["rel_true_res"] < 1e-9 * 1.01
+    sysm.close()
+
+
+def test_split_precision_unsupported_preconditioner():
+    A, b = gen.grid2d_unit(16, seed=3)
+    sysm = gb.System.from_csr(A, "line_jacobi")
+    with pytest.raises(RuntimeError):
+        sysm.solve(dev(b), precision=2)
+    sysm.close()
+
+
 def test_host_buffers_solve():
     A, b = gen.grid2d_unit(40, seed=5)
     ref = oracle.solve(A.n, A.ia, A.ja, A.a, b, "ichol", 1e-10, 3000)
