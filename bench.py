@@ -3,10 +3,14 @@
 Workload (one "step" = one full solve from x0 = 0):
   128^3 7-point Laplacian, edge weights lognormal(0, 0.5), + 1e-3 I (n = 2,097,152,
   nnz = 14,581,760), b ~ U[-1,1] (seed 1002), IC(0), tol 1e-8 relative to ||b||.
-  value  = mixed precision (FP32 inner PCG, FP64 iterative refinement) solve time,
-           device-resident inputs, CUDA events on the solver stream;
+  value  = mixed-precision solve time, precision=2: FP64 Krylov recurrence
+           (x, r, p, q, alpha, beta) around the FP32 SpMV and the FP32 IC(0)
+           triangular solves, with FP64 residual replacement; device-resident
+           inputs, CUDA events on the solver stream;
   fp64   = the plain FP64 device PCG on the same system (the comparator the
            metric names);
+  fp32_krylov = precision=1: FP32 Krylov vectors, SpMV and IC(0) inside FP64
+           iterative refinement (reported beside; needs ~1.75x the iterations);
   e2e    = the same mixed solve through gb_pcg_solve_host from pinned host
            buffers (b, x0 in; x out), copies inside the timed region.
 Inputs (matrix 175 MB FP64 + 117 MB FP32 copy + factors) exceed the 129 MB L2,
@@ -35,6 +39,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "time to rel-res 1e-8, mixed-prec IC0-PCG on 128^3 Laplacian (1 GB300)"
+MIXED = 2  # the headline mixed-precision mode (gb_pcg_opts.precision)
 UNIT = "ms"
 WORKLOAD = "grid3d_lognormal_128 (n=2097152, nnz=14581760), IC0, tol 1e-8"
 
@@ -189,6 +194,22 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_kernels_only(args, local):
+    """Per-kernel device times of PCG iterations run eagerly (no graph), for
+    each precision mode -- the launches a profiler can attribute one by one."""
+    import torch
+
+    import lap_gb300 as gb
+
+    torch.cuda.set_device(local)
+    A, b = make_workload(args.size)
+    sysm = gb.System.from_csr(A, "ichol")
+    db = torch.from_numpy(b).cuda()
+    out = {p: [(k["name"], round(k["ms"], 5)) for k in sysm.profile(db, precision=p, iters=args.profile_iters)]
+           for p in (0, 1, 2)}
+    print(json.dumps({"kernels_only": out, "n": A.n, "nnz": A.nnz}), flush=True)
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -204,8 +225,9 @@ def run_ours(args, world, rank, local):
 
     # warm-up: graphs captured, clocks up
     for _ in range(args.warmup):
-        sysm.solve(db, precision=1, **kw)
+        sysm.solve(db, precision=MIXED, **kw)
         sysm.solve(db, precision=0, **kw)
+    sysm.solve(db, precision=1, **kw)
 
     def timed(precision, steps):
         ms, res = [], None
@@ -220,9 +242,11 @@ def run_ours(args, world, rank, local):
 
     with ClockSampler(local) as clk:
         t0 = time.time()
-        ms_mixed, r_mixed, x_mixed = timed(1, args.steps)
+        ms_mixed, r_mixed, x_mixed = timed(MIXED, args.steps)
         wall = time.time() - t0
     ms_fp64, r_fp64, x_fp64 = timed(0, max(2, args.steps // 2))
+    ms_f32k, r_f32k, _ = timed(1, 2)
+    err_vs_fp64 = float(torch.linalg.norm(x_mixed - x_fp64) / torch.linalg.norm(x_fp64))
 
     # end to end from pinned host buffers
     bh = torch.from_numpy(b).pin_memory()
@@ -231,55 +255,70 @@ def run_ours(args, world, rank, local):
     for _ in range(args.steps):
         xh.zero_()
         r = gb.PcgResult()
-        o = gb.opts(precision=1, **kw)
+        o = gb.opts(precision=MIXED, **kw)
         gb.check(gb.lib().gb_pcg_solve_host(sysm.h, bh.data_ptr(), xh.data_ptr(), gb.C.byref(o),
                                             gb.C.byref(r)), "gb_pcg_solve_host")
         e2e.append(r.device_ms)
 
     # per-kernel device time of one iteration (CUDA events on the solver stream)
     peak, peak_kind = measured_peak()
-    prof = {p: sysm.profile(db, precision=p, iters=20) for p in (0, 1)}
+    pname = {0: "fp64", 1: "fp32-krylov", 2: "split"}
+    prof = {p: sysm.profile(db, precision=p, iters=20) for p in (0, 1, 2)}
     traffic = ncu_traffic()
     kernels = []
     for p, lst in prof.items():
         for k in lst:
             gbs = k["bytes"] / (k["ms"] * 1e-3) / 1e9 if k["ms"] > 0 else 0.0
-            kernels.append({"kernel": k["name"], "precision": "mixed-fp32" if p else "fp64",
+            kernels.append({"kernel": k["name"], "precision": pname[p],
                             "ms": round(k["ms"], 5), "bytes": k["bytes"], "gbs": round(gbs, 1),
                             "frac": round(gbs / peak, 4)})
-    mixed_k = [k for k in kernels if k["precision"] == "mixed-fp32"]
-    dom = max(mixed_k, key=lambda k: k["ms"])
-    tr = traffic.get(f"{dom['kernel']}:{dom['precision']}")
-    roofline = {"bound": "hbm", "kernel": dom["kernel"], "achieved": dom["gbs"], "peak": peak,
-                "unit": "GB/s", "frac": dom["frac"], "traffic": tr,
-                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s"}
+    src = f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s"
+
+    def roof(k):
+        return {"bound": "hbm", "kernel": k["kernel"], "precision": k["precision"],
+                "achieved": k["gbs"], "peak": peak, "unit": "GB/s", "frac": k["frac"],
+                "traffic": traffic.get(f"{k['kernel']}:{k['precision']}"), "peak_source": src}
+
+    mixed_k = [k for k in kernels if k["precision"] == pname[MIXED]]
+    dom = max(mixed_k, key=lambda k: k["ms"])  # a triangular solve: dependency-latency bound
+    roofline = roof(dom)
+    # the bandwidth-bound kernels of the same iteration (SpMV + fused vector updates)
+    bw = {k["kernel"]: roof(k) for k in kernels
+          if k["precision"] in ("fp64", pname[MIXED]) and k["kernel"] in ("spmv_pq", "spmv_pq_split", "update")}
 
     v = allmax(world, statistics.mean(ms_mixed))
     v64 = allmax(world, statistics.mean(ms_fp64))
+    v32k = allmax(world, statistics.mean(ms_f32k))
     ve2e = allmax(world, statistics.mean(e2e))
     if rank != 0:
         return
     it_in, outer = r_mixed["iters"], r_mixed["outer"]
-    # kernels per solve: FP64 = prologue 3 + 3/iteration (+ the final no-op body) + true residual;
-    # mixed = per refinement step (outer residual + prologue 3 + 3/iteration + correction)
-    launches_mixed = it_in * 3 + outer * (1 + 3 + 3 + 1) + 1 + 1
+    # our kernels per split-precision solve: first outer residual 1, prologue 4
+    # (residual, sentinel fill, lower, upper), 4 per iteration (one graph body:
+    # spmv_pq_split, update, lower, upper), an outer residual after each of the
+    # `outer` pauses, 4 per resume (resume, fill, lower, upper; all pauses but
+    # the last), final true residual 1
+    launches_mixed = 1 + 4 + 4 * it_in + outer + 4 * max(outer - 1, 0) + 1
     line = {"metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v, 4),
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 inner / f64 refinement", "data": "synthetic (seeded generator, no dataset)",
+            "dtype": "f32 SpMV + IC0 solves / f64 Krylov recurrence", "data": "synthetic (seeded generator, no dataset)",
             "config": {"workload": WORKLOAD, "n": n, "nnz": nnz, "preconditioner": "ichol",
-                       "precision": "FP32 inner PCG + FP64 iterative refinement",
+                       "precision": "FP64 PCG recurrence around FP32 SpMV and FP32 IC(0) triangular "
+                                    "solves, FP64 residual replacement (gb_pcg_opts.precision=2)",
                        "l2": "inputs larger than L2 (no flush)",
                        "lower_levels": info["lower_levels"], "upper_levels": info["upper_levels"],
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "mixed": {"ms": round(v, 4), "inner_iters": it_in, "outer": outer,
-                      "rel_true_res": r_mixed["rel_true_res"]},
+            "mixed": {"ms": round(v, 4), "iters": it_in, "replacements": outer,
+                      "rel_true_res": r_mixed["rel_true_res"], "rel_err_vs_fp64_solution": err_vs_fp64},
             "fp64": {"ms": round(v64, 4), "iters": r_fp64["iters"], "rel_true_res": r_fp64["rel_true_res"]},
+            "fp32_krylov": {"ms": round(v32k, 4), "iters": r_f32k["iters"], "outer": r_f32k["outer"],
+                            "rel_true_res": r_f32k["rel_true_res"]},
             "speedup_mixed_vs_fp64": round(v64 / v, 3),
             "solves_per_s_all_gpus": round(world * 1e3 / v, 3),
             "e2e": {"value": round(ve2e, 4), "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * n,
                     "d2h_bytes_per_step": 8 * n},
-            "roofline": roofline, "kernels": kernels,
+            "roofline": roofline, "roofline_bandwidth_kernels": bw, "kernels": kernels,
             "gpu_launches": launches_mixed * args.steps,
             "clocks": clk.summary(), "wall_s_timed": round(wall, 3)}
     if world == 1 and not args.no_cpu_baseline:
@@ -297,11 +336,16 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--sample-iters", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="only the eager per-kernel profile of each precision mode (for ncu)")
+    ap.add_argument("--profile-iters", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_init(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.kernels_only:
+        run_kernels_only(args, local)
     else:
         import __graft_entry__
 
