@@ -20,7 +20,7 @@
  *     triangle receives L, diagonal included) and cuda_ichol applies
  *     (L L^T)^{-1} reading pdata->ichol_vals with A's ia/ja, as
  *     cuda_blas.cu:261-561 does.
- * Differences (fixes), all documented in DESIGN.md: memcpyDevice "D2D" is a
+ * Deliberate differences (fixes): memcpyDevice "D2D" is a
  * device-to-device copy; allocation failures are reported on stderr and
  * return NULL; prec_function reports an unknown name on stderr.
  */

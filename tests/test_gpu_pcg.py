@@ -23,7 +23,7 @@ import lap_gb300 as gb  # noqa: E402
 import oracle  # noqa: E402
 from lap_gb300 import gen  # noqa: E402
 
-X_TOL = 1e-6  # solution tolerance vs the reference (spec acceptance)
+X_TOL = 1e-6  # solution tolerance vs the reference (the acceptance bar)
 
 
 def dev(a):
