@@ -133,23 +133,31 @@ int gb_adjoint_grad(gb_system sys, const double *x, const double *g, double *lam
 
 /* ------------------------------------------------------------ batching */
 typedef struct gb_batch_s *gb_batch;
-/* count independent CSR systems concatenated block-diagonally: row_off[count+1]
- * and nnz_off[count+1] (host, int64) give each system's rows / entries in the
- * concatenated ia (local 0-based row pointers per system, each starting at 0),
- * ja (local column indices) and a arrays.  Preconditioner: "line_jacobi". */
+/* count independent CSR systems concatenated block-diagonally (device arrays):
+ * ia holds the N+1 row pointers of the concatenation (N = row_off[count]),
+ * ja each entry's column index LOCAL to its system (0-based), a the values.
+ * row_off[count+1] and nnz_off[count+1] (host, int64) give each system's
+ * first row and first entry; ia[row_off[s]] must equal nnz_off[s].  Every
+ * row needs a nonzero diagonal.  Preconditioner: "line_jacobi" or "none".
+ * The arrays are borrowed and must outlive the batch. */
 int gb_batch_create(int count, const long long *row_off_host, const long long *nnz_off_host,
                     const int *ia, const int *ja, const double *a, const char *prec_name,
                     gb_batch *out);
 int gb_batch_destroy(gb_batch batch);
-/* Solves every system; b, x concatenated.  iters_host / flags_host (may be
- * NULL) receive per-system iteration counts and cg.c flags.  The tile and
- * row-bundle shape is chosen by the autotuner on first use. */
+/* Solves every system in one persistent launch (a CUDA graph whose while
+ * node runs until every system stopped); b, x concatenated [N], x holds x0.
+ * opts->precision 0 (FP64) or 2 (FP32 matrix values and products inside the
+ * FP64 recurrence with per-system residual replacement).  iters_host /
+ * flags_host (may be NULL) receive per-system iteration counts and cg.c
+ * flags; result aggregates them (maximum iterations, worst flag, largest
+ * true residual). */
 int gb_batch_solve(gb_batch batch, const double *b, double *x, const gb_pcg_opts *opts,
                    int *iters_host, int *flags_host, gb_pcg_result *result);
 
-/* Multi-RHS: nrhs right-hand sides on one system, b and x row-major
- * [nrhs][n].  Each column runs its own PCG recurrence; the matrix is read
- * once per iteration for all columns. */
+/* Multi-RHS: nrhs right-hand sides on one system, B and X row-major
+ * [nrhs][n] (X holds x0).  Each column runs its own PCG recurrence in the
+ * batch engine above; the matrix is read once per iteration for all
+ * columns.  Systems with "line_jacobi" or "none"; precision 0 or 2. */
 int gb_pcg_solve_multi(gb_system sys, int nrhs, const double *B, double *X,
                        const gb_pcg_opts *opts, int *iters_host, gb_pcg_result *result);
 

@@ -293,3 +293,74 @@ class System:
         k = cnt.value
         return [dict(name=nm, ms=float(ms[i]), bytes=float(by[i]))
                 for i, nm in enumerate(names.value.decode().split(";")[:k])]
+
+
+class Batch:
+    """Many independent CSR systems solved together (gb_batch_*): the
+    matrices are concatenated block-diagonally with system-local columns."""
+
+    def __init__(self, mats, prec="line_jacobi"):
+        import torch
+
+        row_off = np.zeros(len(mats) + 1, dtype=np.int64)
+        nnz_off = np.zeros(len(mats) + 1, dtype=np.int64)
+        for s, A in enumerate(mats):
+            row_off[s + 1] = row_off[s] + A.n
+            nnz_off[s + 1] = nnz_off[s] + A.nnz
+        ia = np.concatenate([A.ia[:-1] + nnz_off[s] for s, A in enumerate(mats)] + [nnz_off[-1:]])
+        self.ia = torch.from_numpy(ia.astype(np.int32)).cuda()
+        self.ja = torch.from_numpy(np.concatenate([A.ja for A in mats]).astype(np.int32)).cuda()
+        self.a = torch.from_numpy(np.concatenate([A.a for A in mats]).astype(np.float64)).cuda()
+        self.row_off, self.nnz_off = row_off, nnz_off
+        self.count, self.N = len(mats), int(row_off[-1])
+        h = C.c_void_p()
+        check(lib().gb_batch_create(self.count, row_off.ctypes.data, nnz_off.ctypes.data, ptr(self.ia),
+                                    ptr(self.ja), ptr(self.a), prec.encode(), C.byref(h)), "gb_batch_create")
+        self.h = h
+
+    def solve(self, b, x=None, **kw):
+        """b, x: concatenated device vectors [N].  Returns (x, per-system
+        iterations, per-system flags, aggregate result dict)."""
+        import torch
+
+        b = b.to(device="cuda", dtype=torch.float64).contiguous()
+        x = torch.zeros_like(b) if x is None else x.to(device="cuda", dtype=torch.float64).contiguous().clone()
+        o = opts(**kw)
+        r = PcgResult()
+        it = np.zeros(self.count, dtype=np.int32)
+        fl = np.zeros(self.count, dtype=np.int32)
+        torch.cuda.synchronize()
+        check(lib().gb_batch_solve(self.h, ptr(b), ptr(x), C.byref(o), it.ctypes.data, fl.ctypes.data,
+                                   C.byref(r)), "gb_batch_solve")
+        return x, it, fl, r.as_dict()
+
+    def split(self, v):
+        """Per-system views of a concatenated vector."""
+        return [v[self.row_off[s]:self.row_off[s + 1]] for s in range(self.count)]
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().gb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve_multi(system, B, X=None, **kw):
+    """nrhs right-hand sides on one System (gb_pcg_solve_multi); B [nrhs, n]
+    on the device.  Returns (X, per-column iterations, aggregate result)."""
+    import torch
+
+    B = B.to(device="cuda", dtype=torch.float64).contiguous()
+    X = torch.zeros_like(B) if X is None else X.to(device="cuda", dtype=torch.float64).contiguous().clone()
+    o = opts(**kw)
+    r = PcgResult()
+    it = np.zeros(B.shape[0], dtype=np.int32)
+    torch.cuda.synchronize()
+    check(lib().gb_pcg_solve_multi(system.h, B.shape[0], ptr(B), ptr(X), C.byref(o), it.ctypes.data,
+                                   C.byref(r)), "gb_pcg_solve_multi")
+    return X, it, r.as_dict()

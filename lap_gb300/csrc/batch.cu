@@ -1,0 +1,866 @@
+// batch.cu -- many PCG systems in one persistent CUDA-graph launch.
+//
+// A batch is S independent systems whose vectors are concatenated:
+//   * block-diagonal: S Laplacians of uneven size (gb_batch_create), their
+//     CSR concatenated with global row pointers and system-local columns;
+//   * multi-RHS: S right-hand sides on one gb_system (gb_pcg_solve_multi),
+//     the matrix shared and read once per iteration for all columns.
+// Each system runs its own PCG recurrence of cg.c:42-126 -- its own alpha,
+// beta, rho, stopping test and flag -- held in one PcgState per system, so
+// the single-system building blocks (pcg_alpha, pcg_check) apply unchanged.
+// One iteration of all systems is four launches:
+//   bspmv_pq      q = A w + beta q, p = w + beta p; p'q per bundle
+//   breduce_alpha per system: p'q in bundle order, alpha (breakdown test)
+//   bupdate       x += alpha p, r -= alpha q, w = M^-1 r; r'r, r'w per chunk
+//   breduce_check per system: the stopping test; counts the systems still
+//                 running and ends the graph's while loop when none is
+// Reductions are segmented and in fixed order (partials per bundle / chunk,
+// summed by one warp per system), so results are reproducible.  A system
+// that stopped costs one flag read per bundle.  Preconditioners: line_jacobi
+// (y = D^-1 x, line_jacobi.c:3-7) and none.
+//
+// precision 2 (split): FP32 matrix values and FP32 products A w around the
+// FP64 recurrence; a system whose recursive residual has dropped by
+// inner_tol (never below its target) pauses, its residual is replaced by the
+// FP64 b - A x, and it resumes with p, q and rho kept -- the same scheme as
+// the single-system split solve, per system.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gb_common.cuh"
+#include "gblap.h"
+#include "kernels.h"
+#include "pcg.h"
+#include "pcg_state.cuh"
+#include "system.h"
+
+namespace gb {
+
+constexpr int kBatchThreads = 256;
+constexpr int kBatchWarps = kBatchThreads / 32;
+constexpr int kChunkRows = 2048;  // rows of one update / reduction chunk
+
+struct BatchArgs {
+  int count, N, n1, nb, nc, shared, jacobi;
+  const int* ia;
+  const int* ja;
+  const int* bundles;   // bundle row starts (global rows, or the shared matrix's rows)
+  const int* bsys;      // block-diagonal: system of each bundle
+  const int* sys_b;     // block-diagonal: [count+1] bundle range of each system
+  const int* chunk_r0;  // [nc+1] chunk row starts (global rows)
+  const int* csys;      // [nc] system of each chunk
+  const int* sys_c;     // [count+1] chunk range of each system
+  const int* row_off;   // [count+1] first row of each system
+  const double* a;
+  const float* a32;
+  const double* d_r;    // [N] (block-diagonal) or [n1] (shared)
+  const double* b;
+  double *x, *r, *w, *p, *q;
+  PcgState* st;         // [count] recurrence
+  PcgState* so;         // [count] outer (split precision): target and final state
+  double* part_b;       // [3 * nb * (shared ? count : 1)]
+  double* part_c;       // [2 * nc]
+  unsigned* tk;         // [0] check ticket, [1] outer ticket, [2] loop guard
+  int* nactive;         // [0] running systems, [1] systems to resume
+  int maxit;
+};
+
+// x operand of the system whose vectors start at `off`, rounded to the
+// matrix's type (FP32 products in the split precision)
+template <typename TA>
+struct XOff {
+  const double* __restrict__ x;
+  __device__ __forceinline__ TA operator()(int c) const { return (TA)__ldg(x + c); }
+};
+
+__device__ __forceinline__ int sys_bundle_begin(const BatchArgs& B, int s) {
+  return B.shared ? s * B.nb : B.sys_b[s];
+}
+__device__ __forceinline__ int sys_bundle_end(const BatchArgs& B, int s) {
+  return B.shared ? (s + 1) * B.nb : B.sys_b[s + 1];
+}
+__device__ __forceinline__ double dr_at(const BatchArgs& B, int s, int i) {
+  return B.shared ? B.d_r[i - s * B.n1] : B.d_r[i];
+}
+
+// Runs `body(s, slot, off)` for every (bundle, system) pair of this warp's
+// share: block-diagonal bundles belong to one system; a shared-matrix bundle
+// is visited once per system (its entries stay in L1 across the visits).
+template <typename F>
+__device__ __forceinline__ void for_bundles(const BatchArgs& B, F&& body) {
+  const int warps = gridDim.x * kBatchWarps;
+  for (int bb = blockIdx.x * kBatchWarps + (threadIdx.x >> 5); bb < B.nb; bb += warps) {
+    if (!B.shared) {
+      body(bb, B.bsys[bb], bb, 0);
+    } else {
+      for (int s = 0; s < B.count; ++s) body(bb, s, s * B.nb + bb, s * B.n1);
+    }
+  }
+}
+
+// ------------------------------------------------------------ prologue
+// r = b - A x, w = M^-1 r; per bundle: r'r, r'w.
+__global__ void __launch_bounds__(kBatchThreads) bresid_kernel(BatchArgs B) {
+  __shared__ double stage[kBatchWarps][kBundleNnz];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for_bundles(B, [&](int bb, int s, int slot, int off) {
+    struct Ep {
+      const BatchArgs& B;
+      int s, off;
+      double a0, a1;
+      __device__ double init(int) const { return 0.0; }
+      __device__ void store(int row, double v) {
+        const int i = off + row;
+        const double ri = B.b[i] - v;
+        const double wi = B.jacobi ? dr_at(B, s, i) * ri : ri;
+        B.r[i] = ri;
+        B.w[i] = wi;
+        a0 += ri * ri;
+        a1 += ri * wi;
+      }
+    } ep{B, s, off, 0.0, 0.0};
+    XOff<double> xf{B.x + (B.shared ? off : B.row_off[s])};
+    spmv_bundle<double, false>(bb, B.shared ? B.n1 : B.N, B.bundles, B.ia, B.ja, B.a, 1.0, xf, ep,
+                               stage[wid]);
+    const double s0 = warp_sum(ep.a0), s1 = warp_sum(ep.a1);
+    if (lane == 0) {
+      B.part_b[3 * slot] = s0;
+      B.part_b[3 * slot + 1] = s1;
+    }
+  });
+}
+
+// Per system: ||r0||, the stopping threshold, rho.
+__global__ void __launch_bounds__(kBatchThreads) breduce_init_kernel(BatchArgs B) {
+  const int lane = threadIdx.x & 31;
+  const int s = blockIdx.x * kBatchWarps + (threadIdx.x >> 5);
+  if (s >= B.count) return;
+  double v0 = 0.0, v1 = 0.0;
+  for (int i = sys_bundle_begin(B, s) + lane; i < sys_bundle_end(B, s); i += 32) {
+    v0 += B.part_b[3 * i];
+    v1 += B.part_b[3 * i + 1];
+  }
+  v0 = warp_sum(v0);
+  v1 = warp_sum(v1);
+  if (lane == 0) {
+    PcgState& S = B.st[s];
+    const double res0 = sqrt(v0);
+    S.res0 = res0;
+    S.rr = v0;
+    S.tolrel = S.spare0 * res0;  // spare0 carries this recurrence's tolerance
+    S.rho = B.jacobi ? v1 : v0;
+    S.rho_prev = 0.0;
+  }
+}
+
+// ------------------------------------------------------------ iteration
+template <typename TA>
+__global__ void __launch_bounds__(kBatchThreads)
+    bspmv_pq_kernel(BatchArgs B, const TA* __restrict__ a, cudaGraphConditionalHandle cond, int has_cond) {
+  __shared__ TA stage[kBatchWarps][kBundleNnz];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // loop guard, independent of the checking kernel
+  if (has_cond && blockIdx.x == 0 && threadIdx.x == 0) {
+    const unsigned g = atomicAdd(&B.tk[2], 1u) + 1u;
+    if (g > (unsigned)B.maxit + 8u) set_cond(cond, true, false);
+  }
+  for_bundles(B, [&](int bb, int s, int slot, int off) {
+    const PcgState& S = B.st[s];
+    if (S.done) return;  // uniform in the warp
+    const double beta = S.iter == 0 ? 0.0 : S.rho / S.rho_prev;
+    const bool first = S.iter == 0;
+    struct Ep {
+      const BatchArgs& B;
+      int off;
+      double beta;
+      bool first;
+      double pq;
+      __device__ TA init(int) const { return TA(0); }
+      __device__ void store(int row, TA v) {
+        const int i = off + row;
+        const double wi = B.w[i];
+        const double pi = first ? wi : fma_rn(beta, B.p[i], wi);
+        const double qi = first ? (double)v : fma_rn(beta, B.q[i], (double)v);
+        B.p[i] = pi;
+        B.q[i] = qi;
+        pq = fma_rn(pi, qi, pq);
+      }
+    } ep{B, off, beta, first, 0.0};
+    XOff<TA> xf{B.w + (B.shared ? off : B.row_off[s])};
+    spmv_bundle<TA, false>(bb, B.shared ? B.n1 : B.N, B.bundles, B.ia, B.ja, a, TA(1), xf, ep,
+                           stage[wid]);
+    const double v = warp_sum(ep.pq);
+    if (lane == 0) B.part_b[3 * slot] = v;
+  });
+}
+
+__global__ void __launch_bounds__(kBatchThreads) breduce_alpha_kernel(BatchArgs B) {
+  const int lane = threadIdx.x & 31;
+  const int s = blockIdx.x * kBatchWarps + (threadIdx.x >> 5);
+  if (s >= B.count) return;
+  PcgState& S = B.st[s];
+  if (S.done) return;
+  double v = 0.0;
+  for (int i = sys_bundle_begin(B, s) + lane; i < sys_bundle_end(B, s); i += 32) v += B.part_b[3 * i];
+  v = warp_sum(v);
+  if (lane == 0) {
+    S.pq = v;
+    double alpha;
+    if (!pcg_alpha(&S, &alpha)) {
+      S.done = 1;
+      S.flag = 2;
+      S.status = GB_BREAKDOWN;
+    }
+    S.spare1 = alpha;
+  }
+}
+
+__global__ void __launch_bounds__(kBatchThreads) bupdate_kernel(BatchArgs B) {
+  __shared__ double sm[2 * kBatchWarps];
+  for (int c = blockIdx.x; c < B.nc; c += gridDim.x) {
+    const int s = B.csys[c];
+    const PcgState& S = B.st[s];
+    if (S.done) continue;  // uniform in the block
+    const double al = S.spare1;
+    const int r0 = B.chunk_r0[c], r1 = B.chunk_r0[c + 1];
+    double acc[2] = {0.0, 0.0};
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+      B.x[i] = fma_rn(al, B.p[i], B.x[i]);
+      const double ri = fma_rn(-al, B.q[i], B.r[i]);
+      const double wi = B.jacobi ? dr_at(B, s, i) * ri : ri;
+      B.r[i] = ri;
+      B.w[i] = wi;
+      acc[0] = fma_rn(ri, ri, acc[0]);
+      acc[1] = fma_rn(ri, wi, acc[1]);
+    }
+    block_sum<2>(acc, sm);
+    if (threadIdx.x == 0) {
+      B.part_c[2 * c] = acc[0];
+      B.part_c[2 * c + 1] = acc[1];
+    }
+    __syncthreads();  // sm reused by the next chunk
+  }
+}
+
+// Counts the systems still running (lane 0 of each live system's warp);
+// the last block to finish decides whether the loop continues.
+__device__ __forceinline__ void batch_loop_decide(const BatchArgs& B, cudaGraphConditionalHandle cond,
+                                                  int has_cond) {
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(&B.tk[0], 1u) == gridDim.x - 1u;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    const int live = atomicExch(&B.nactive[0], 0);
+    B.nactive[2] = live;  // read by the host-driven (eager) loop
+    B.tk[0] = 0u;
+    const bool guard_ok = *(volatile unsigned*)&B.tk[2] <= (unsigned)B.maxit + 4u;
+    set_cond(cond, has_cond, live > 0 && guard_ok);
+    __threadfence();
+  }
+}
+
+__global__ void __launch_bounds__(kBatchThreads)
+    breduce_check_kernel(BatchArgs B, cudaGraphConditionalHandle cond, int has_cond) {
+  const int lane = threadIdx.x & 31;
+  const int s = blockIdx.x * kBatchWarps + (threadIdx.x >> 5);
+  if (s < B.count && !B.st[s].done) {
+    PcgState& S = B.st[s];
+    double v0 = 0.0, v1 = 0.0;
+    for (int c = B.sys_c[s] + lane; c < B.sys_c[s + 1]; c += 32) {
+      v0 += B.part_c[2 * c];
+      v1 += B.part_c[2 * c + 1];
+    }
+    v0 = warp_sum(v0);
+    v1 = warp_sum(v1);
+    if (lane == 0) {
+      pcg_check(&S, v0, nullptr);  // hist_len is 0 for batch systems
+      if (!S.done) {
+        S.rho_prev = S.rho;
+        S.rho = B.jacobi ? v1 : v0;
+        atomicAdd(&B.nactive[0], 1);
+      }
+    }
+  }
+  batch_loop_decide(B, cond, has_cond);
+}
+
+// ------------------------------------------------------------ true residuals
+// replace = 1 (split precision): for every system whose recurrence paused
+// converged and is not final, r = b - A x in FP64 and w = M^-1 r (the
+// replacement); partials ||r||^2, r'w.  replace = 0 (report): ||b - A x||^2
+// and ||b||^2 of every system, nothing written.
+__device__ __forceinline__ bool batch_needs_check(const BatchArgs& B, int s) {
+  return B.st[s].done && B.st[s].flag == 0 && !B.so[s].done;
+}
+
+__global__ void __launch_bounds__(kBatchThreads) btrue_kernel(BatchArgs B, int replace) {
+  __shared__ double stage[kBatchWarps][kBundleNnz];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for_bundles(B, [&](int bb, int s, int slot, int off) {
+    if (replace && !batch_needs_check(B, s)) return;
+    struct Ep {
+      const BatchArgs& B;
+      int s, off, replace;
+      double a0, a1, a2;
+      __device__ double init(int) const { return 0.0; }
+      __device__ void store(int row, double v) {
+        const int i = off + row;
+        const double bi = B.b[i], ri = bi - v;
+        a0 += ri * ri;
+        a2 += bi * bi;
+        if (replace) {
+          const double wi = B.jacobi ? dr_at(B, s, i) * ri : ri;
+          B.r[i] = ri;
+          B.w[i] = wi;
+          a1 += ri * wi;
+        }
+      }
+    } ep{B, s, off, replace, 0.0, 0.0, 0.0};
+    XOff<double> xf{B.x + (B.shared ? off : B.row_off[s])};
+    spmv_bundle<double, false>(bb, B.shared ? B.n1 : B.N, B.bundles, B.ia, B.ja, B.a, 1.0, xf, ep,
+                               stage[wid]);
+    const double v0 = warp_sum(ep.a0), v1 = warp_sum(ep.a1), v2 = warp_sum(ep.a2);
+    if (lane == 0) {
+      B.part_b[3 * slot] = v0;
+      B.part_b[3 * slot + 1] = v1;
+      B.part_b[3 * slot + 2] = v2;
+    }
+  });
+}
+
+// replace = 1: the refinement decision per checked system -- final when the
+// FP64 residual meets the target (or replacements ran out), otherwise the
+// recurrence resumes with the threshold max(delta*||r||, target) and rho of
+// the replaced residual; nactive[1] counts the resumed systems.
+// replace = 0: stores ||b - A x|| in so.spare1 and ||b|| in so.rho.
+__global__ void __launch_bounds__(kBatchThreads)
+    breduce_outer_kernel(BatchArgs B, int replace, double delta, int max_outer) {
+  const int lane = threadIdx.x & 31;
+  const int s = blockIdx.x * kBatchWarps + (threadIdx.x >> 5);
+  if (s >= B.count) return;
+  PcgState& S = B.st[s];
+  PcgState& O = B.so[s];
+  if (replace && !batch_needs_check(B, s)) {
+    // a recurrence that stopped on maxit or breakdown is final as it is
+    if (lane == 0 && S.done && !O.done) {
+      O.done = 1;
+      O.flag = S.flag;
+      O.status = S.status;
+    }
+    return;
+  }
+  double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+  for (int i = sys_bundle_begin(B, s) + lane; i < sys_bundle_end(B, s); i += 32) {
+    v0 += B.part_b[3 * i];
+    v1 += B.part_b[3 * i + 1];
+    v2 += B.part_b[3 * i + 2];
+  }
+  v0 = warp_sum(v0);
+  v1 = warp_sum(v1);
+  v2 = warp_sum(v2);
+  if (lane != 0) return;
+  const double rt = sqrt(v0);
+  if (!replace) {
+    O.spare1 = rt;
+    O.rho = sqrt(v2);
+    return;
+  }
+  O.rr = v0;
+  O.iter += 1;  // replacements
+  if (!(rt == rt) || isinf(rt)) {
+    O.done = 1;
+    O.flag = 2;
+    O.status = GB_BREAKDOWN;
+  } else if (rt < O.tolrel) {
+    O.done = 1;
+    O.flag = 0;
+    O.status = GB_OK;
+  } else if (O.iter >= max_outer || S.iter > S.maxit) {
+    O.done = 1;
+    O.flag = 1;
+    O.status = GB_MAXIT;
+  } else {
+    S.done = 0;
+    S.flag = 1;
+    S.status = GB_OK;
+    S.tolrel = fmax(delta * rt, O.tolrel);
+    S.rho_prev = S.rho;
+    S.rho = B.jacobi ? v1 : v0;
+    atomicAdd(&B.nactive[1], 1);
+  }
+}
+
+// target of the refinement: tol * ||b - A x0|| (the recurrence's res0)
+__global__ void batch_target_kernel(BatchArgs B) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= B.count) return;
+  B.so[s].res0 = B.st[s].res0;
+  B.so[s].tolrel = B.so[s].spare0 * B.st[s].res0;
+}
+
+// 1 / diagonal of every row of a block-diagonal batch (the system-local
+// column equal to the row's local index); a missing or zero diagonal is
+// reported as its global row + 1.
+__global__ void batch_diag_kernel(BatchArgs B, double* d_r, int* bad) {
+  for (int c = blockIdx.x; c < B.nc; c += gridDim.x) {
+    const int s = B.csys[c], off = B.row_off[s];
+    for (int i = B.chunk_r0[c] + threadIdx.x; i < B.chunk_r0[c + 1]; i += blockDim.x) {
+      double d = 0.0;
+      for (int k = B.ia[i]; k < B.ia[i + 1]; ++k)
+        if (B.ja[k] == i - off) d = B.a[k];
+      if (d == 0.0) atomicCAS(bad, 0, i + 1);
+      d_r[i] = d != 0.0 ? 1.0 / d : 0.0;
+    }
+  }
+}
+
+}  // namespace gb
+
+// ================================================================ host side
+using namespace gb;
+
+struct gb_batch_s {
+  int count = 0;
+  int shared = 0;  // multi-RHS over one matrix
+  int N = 0;       // rows of all systems (the vectors' length)
+  int n1 = 0;      // rows of the shared matrix
+  int jacobi = 1;
+  cudaStream_t s = nullptr;
+  bool own_stream = false;
+  const int* ia = nullptr;
+  const int* ja = nullptr;
+  const double* a = nullptr;
+  const float* a32 = nullptr;
+  const double* d_r = nullptr;
+  const int* bundles = nullptr;
+  int nb = 0, nc = 0;
+  std::vector<void*> owned;  // device buffers freed with the batch
+  int *row_off = nullptr, *bsys = nullptr, *sys_b = nullptr, *chunk_r0 = nullptr, *csys = nullptr,
+      *sys_c = nullptr;
+  double *b = nullptr, *x = nullptr, *r = nullptr, *w = nullptr, *p = nullptr, *q = nullptr;
+  PcgState *st = nullptr, *so = nullptr, *st_h = nullptr;
+  double *part_b = nullptr, *part_c = nullptr;
+  unsigned* tk = nullptr;
+  int* nactive = nullptr;
+  LoopGraph loop[2];  // [FP64, split]
+  int loop_maxit[2] = {-1, -1};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+template <typename T>
+int balloc(gb_batch bt, T** p, size_t n) {
+  void* v = nullptr;
+  if (cudaMalloc(&v, sizeof(T) * std::max<size_t>(n, 1)) != cudaSuccess) {
+    cudaGetLastError();
+    return GB_NO_MEMORY;
+  }
+  bt->owned.push_back(v);
+  *p = static_cast<T*>(v);
+  return GB_OK;
+}
+
+template <typename T>
+int bupload(gb_batch bt, T** p, const std::vector<T>& h) {
+  GB_TRY(balloc(bt, p, h.size()));
+  GB_CUDA_TRY(cudaMemcpy(*p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
+  return GB_OK;
+}
+
+void batch_free(gb_batch bt) {
+  for (auto& lg : bt->loop) {
+    if (lg.exec) cudaGraphExecDestroy(lg.exec);
+    if (lg.graph) cudaGraphDestroy(lg.graph);
+  }
+  for (void* v : bt->owned) cudaFree(v);
+  if (bt->st_h) cudaFreeHost(bt->st_h);
+  if (bt->ev0) cudaEventDestroy(bt->ev0);
+  if (bt->ev1) cudaEventDestroy(bt->ev1);
+  if (bt->own_stream && bt->s) cudaStreamDestroy(bt->s);
+  delete bt;
+}
+
+// Chunks of <= kChunkRows rows, never across systems; row_off on the host.
+int batch_chunks(gb_batch bt, const std::vector<int>& row_off) {
+  std::vector<int> r0, cs, sc(bt->count + 1, 0);
+  for (int s = 0; s < bt->count; ++s) {
+    sc[s] = (int)cs.size();
+    for (int i = row_off[s]; i < row_off[s + 1]; i += kChunkRows) {
+      r0.push_back(i);
+      cs.push_back(s);
+    }
+  }
+  sc[bt->count] = (int)cs.size();
+  r0.push_back(bt->N);
+  bt->nc = (int)cs.size();
+  GB_TRY(bupload(bt, &bt->chunk_r0, r0));
+  GB_TRY(bupload(bt, &bt->csys, cs));
+  GB_TRY(bupload(bt, &bt->sys_c, sc));
+  GB_TRY(bupload(bt, &bt->row_off, row_off));
+  return GB_OK;
+}
+
+// Vectors, states and partials.
+int batch_buffers(gb_batch bt) {
+  const size_t N = bt->N;
+  for (double** v : {&bt->b, &bt->x, &bt->r, &bt->w, &bt->p, &bt->q}) GB_TRY(balloc(bt, v, N));
+  GB_TRY(balloc(bt, &bt->st, bt->count));
+  GB_TRY(balloc(bt, &bt->so, bt->count));
+  GB_CUDA_TRY(cudaMallocHost(&bt->st_h, sizeof(PcgState) * 2 * bt->count));
+  GB_TRY(balloc(bt, &bt->part_b, 3 * (size_t)bt->nb * (bt->shared ? bt->count : 1)));
+  GB_TRY(balloc(bt, &bt->part_c, 2 * (size_t)bt->nc));
+  GB_TRY(balloc(bt, &bt->tk, 4));
+  GB_TRY(balloc(bt, &bt->nactive, 4));
+  GB_CUDA_TRY(cudaMemset(bt->tk, 0, sizeof(unsigned) * 4));
+  GB_CUDA_TRY(cudaMemset(bt->nactive, 0, sizeof(int) * 4));
+  GB_CUDA_TRY(cudaEventCreate(&bt->ev0));
+  GB_CUDA_TRY(cudaEventCreate(&bt->ev1));
+  return GB_OK;
+}
+
+BatchArgs batch_args(gb_batch bt, int maxit) {
+  BatchArgs B;
+  memset(&B, 0, sizeof B);
+  B.count = bt->count;
+  B.N = bt->N;
+  B.n1 = bt->n1;
+  B.nb = bt->nb;
+  B.nc = bt->nc;
+  B.shared = bt->shared;
+  B.jacobi = bt->jacobi;
+  B.ia = bt->ia;
+  B.ja = bt->ja;
+  B.bundles = bt->bundles;
+  B.bsys = bt->bsys;
+  B.sys_b = bt->sys_b;
+  B.chunk_r0 = bt->chunk_r0;
+  B.csys = bt->csys;
+  B.sys_c = bt->sys_c;
+  B.row_off = bt->row_off;
+  B.a = bt->a;
+  B.a32 = bt->a32;
+  B.d_r = bt->d_r;
+  B.b = bt->b;
+  B.x = bt->x;
+  B.r = bt->r;
+  B.w = bt->w;
+  B.p = bt->p;
+  B.q = bt->q;
+  B.st = bt->st;
+  B.so = bt->so;
+  B.part_b = bt->part_b;
+  B.part_c = bt->part_c;
+  B.tk = bt->tk;
+  B.nactive = bt->nactive;
+  B.maxit = maxit;
+  return B;
+}
+
+int grid_bundles(const void* k, int nb, int count, int shared) {
+  const long long warps = (long long)nb * (shared ? 1 : 1);
+  const long long cap = (long long)device_sm_count() * occupancy_blocks(k, kBatchThreads);
+  (void)count;
+  return (int)std::max(1LL, std::min(cap, (warps + kBatchWarps - 1) / kBatchWarps));
+}
+int grid_sys(int count) { return std::max(1, ceil_div(count, kBatchWarps)); }
+int grid_chunks(int nc) {
+  return std::max(1, std::min(nc, device_sm_count() * occupancy_blocks((const void*)bupdate_kernel, kBatchThreads)));
+}
+
+// One iteration of every live system.
+int batch_body(gb_batch bt, int split, int maxit, cudaGraphConditionalHandle cond, int has_cond) {
+  const BatchArgs B = batch_args(bt, maxit);
+  if (split)
+    bspmv_pq_kernel<float><<<grid_bundles((const void*)bspmv_pq_kernel<float>, bt->nb, bt->count, bt->shared),
+                             kBatchThreads, 0, bt->s>>>(B, bt->a32, cond, has_cond);
+  else
+    bspmv_pq_kernel<double><<<grid_bundles((const void*)bspmv_pq_kernel<double>, bt->nb, bt->count, bt->shared),
+                              kBatchThreads, 0, bt->s>>>(B, bt->a, cond, has_cond);
+  GB_CUDA_TRY(cudaGetLastError());
+  breduce_alpha_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B);
+  bupdate_kernel<<<grid_chunks(bt->nc), kBatchThreads, 0, bt->s>>>(B);
+  breduce_check_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B, cond, has_cond);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
+
+// The iteration loop as one graph: a while node around batch_body.
+int batch_loop(gb_batch bt, int split, int maxit, int use_graph) {
+  GB_CUDA_TRY(cudaMemsetAsync(bt->tk, 0, sizeof(unsigned) * 4, bt->s));
+  GB_CUDA_TRY(cudaMemsetAsync(bt->nactive, 0, sizeof(int) * 4, bt->s));
+  if (!use_graph) {
+    for (int it = 0; it <= maxit + 1; it += 16) {
+      for (int j = 0; j < 16; ++j) GB_TRY(batch_body(bt, split, maxit, 0, 0));
+      int live = 0;
+      GB_CUDA_TRY(cudaMemcpyAsync(&live, bt->nactive + 2, sizeof(int), cudaMemcpyDeviceToHost, bt->s));
+      GB_CUDA_TRY(cudaStreamSynchronize(bt->s));
+      if (live == 0) break;
+    }
+    return GB_OK;
+  }
+  LoopGraph& lg = bt->loop[split];
+  if (!lg.exec || bt->loop_maxit[split] != maxit) {
+    if (lg.exec) cudaGraphExecDestroy(lg.exec);
+    if (lg.graph) cudaGraphDestroy(lg.graph);
+    lg = LoopGraph();
+    cudaGraph_t g;
+    GB_CUDA_TRY(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    GB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)];
+    memset(cp_buf, 0, sizeof cp_buf);
+    cudaGraphNodeParams& cp = *reinterpret_cast<cudaGraphNodeParams*>(cp_buf);
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    GB_CUDA_TRY(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
+    GB_CUDA_TRY(cudaStreamBeginCaptureToGraph(bt->s, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal));
+    const int rc = batch_body(bt, split, maxit, h, 1);
+    cudaGraph_t captured = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(bt->s, &captured);
+    if (rc != GB_OK || e != cudaSuccess) {
+      cudaGraphDestroy(g);
+      cudaGetLastError();
+      return rc != GB_OK ? rc : GB_CUDA_ERROR;
+    }
+    GB_CUDA_TRY(cudaGraphInstantiate(&lg.exec, g, 0));
+    lg.graph = g;
+    bt->loop_maxit[split] = maxit;
+  }
+  GB_CUDA_TRY(cudaGraphLaunch(lg.exec, bt->s));
+  return GB_OK;
+}
+
+int batch_solve(gb_batch bt, const double* b, double* x, const gb_pcg_opts* opts, int* iters_host,
+                int* flags_host, gb_pcg_result* res) {
+  gb_pcg_opts o;
+  if (opts) o = *opts;
+  else gb_pcg_opts_default(&o);
+  if (o.precision != 0 && o.precision != 2) return GB_NOT_SUPPORTED;
+  if (o.maxit < 0 || !(o.tol >= 0.0)) return GB_BAD_INPUT;
+  const int split = o.precision == 2;
+  const double itol = o.inner_tol > 0.0 ? o.inner_tol : 1e-2;
+  const size_t bytes = sizeof(double) * (size_t)bt->N;
+  PcgState* hs = bt->st_h;
+  for (int s = 0; s < bt->count; ++s) {
+    PcgState z;
+    memset(&z, 0, sizeof z);
+    z.flag = 1;
+    z.maxit = o.maxit;
+    z.spare0 = split ? std::max(itol, o.tol) : o.tol;
+    hs[s] = z;
+    z.spare0 = o.tol;
+    hs[bt->count + s] = z;
+  }
+  GB_CUDA_TRY(cudaMemcpyAsync(bt->st, hs, sizeof(PcgState) * bt->count, cudaMemcpyHostToDevice, bt->s));
+  GB_CUDA_TRY(cudaMemcpyAsync(bt->so, hs + bt->count, sizeof(PcgState) * bt->count, cudaMemcpyHostToDevice, bt->s));
+  GB_CUDA_TRY(cudaEventRecord(bt->ev0, bt->s));
+  GB_CUDA_TRY(cudaMemcpyAsync(bt->b, b, bytes, cudaMemcpyDeviceToDevice, bt->s));
+  GB_CUDA_TRY(cudaMemcpyAsync(bt->x, x, bytes, cudaMemcpyDeviceToDevice, bt->s));
+  const BatchArgs B = batch_args(bt, o.maxit);
+  const int gb64 = grid_bundles((const void*)bresid_kernel, bt->nb, bt->count, bt->shared);
+  bresid_kernel<<<gb64, kBatchThreads, 0, bt->s>>>(B);
+  breduce_init_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B);
+  batch_target_kernel<<<ceil_div(bt->count, 128), 128, 0, bt->s>>>(B);
+  GB_CUDA_TRY(cudaGetLastError());
+  GB_TRY(batch_loop(bt, split, o.maxit, o.use_graph));
+  if (split) {
+    for (int round = 0; round < o.max_outer + 1; ++round) {
+      GB_CUDA_TRY(cudaMemsetAsync(bt->nactive + 1, 0, sizeof(int), bt->s));
+      btrue_kernel<<<gb64, kBatchThreads, 0, bt->s>>>(B, 1);
+      breduce_outer_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B, 1, itol, o.max_outer);
+      GB_CUDA_TRY(cudaGetLastError());
+      int resumed = 0;
+      GB_CUDA_TRY(cudaMemcpyAsync(&resumed, bt->nactive + 1, sizeof(int), cudaMemcpyDeviceToHost, bt->s));
+      GB_CUDA_TRY(cudaStreamSynchronize(bt->s));
+      if (resumed == 0) break;
+      GB_TRY(batch_loop(bt, split, o.maxit, o.use_graph));
+    }
+  }
+  btrue_kernel<<<gb64, kBatchThreads, 0, bt->s>>>(B, 0);
+  breduce_outer_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B, 0, itol, o.max_outer);
+  GB_CUDA_TRY(cudaGetLastError());
+  GB_CUDA_TRY(cudaMemcpyAsync(x, bt->x, bytes, cudaMemcpyDeviceToDevice, bt->s));
+  GB_CUDA_TRY(cudaEventRecord(bt->ev1, bt->s));
+  GB_CUDA_TRY(cudaMemcpyAsync(hs, bt->st, sizeof(PcgState) * bt->count, cudaMemcpyDeviceToHost, bt->s));
+  GB_CUDA_TRY(cudaMemcpyAsync(hs + bt->count, bt->so, sizeof(PcgState) * bt->count, cudaMemcpyDeviceToHost, bt->s));
+  GB_CUDA_TRY(cudaStreamSynchronize(bt->s));
+  gb_pcg_result r;
+  memset(&r, 0, sizeof r);
+  r.status = GB_OK;
+  for (int s = 0; s < bt->count; ++s) {
+    const PcgState& S = hs[s];
+    const PcgState& O = hs[bt->count + s];
+    const int flag = split ? (O.done ? O.flag : 1) : S.flag;
+    const int status = split ? (O.done ? O.status : GB_MAXIT) : S.status;
+    if (iters_host) iters_host[s] = S.iter;
+    if (flags_host) flags_host[s] = flag;
+    r.iters = std::max(r.iters, S.iter);
+    r.outer = std::max(r.outer, split ? O.iter : 0);
+    r.flag = std::max(r.flag, flag);
+    if (r.status == GB_OK && status != GB_OK) r.status = status;
+    r.res0 = std::max(r.res0, S.res0);
+    r.res = std::max(r.res, split ? std::sqrt(O.rr) : std::sqrt(S.rr));
+    r.true_res = std::max(r.true_res, O.spare1);
+    r.rel_true_res = std::max(r.rel_true_res, O.rho > 0.0 ? O.spare1 / O.rho : O.spare1);
+  }
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, bt->ev0, bt->ev1);
+  r.device_ms = ms;
+  if (res) *res = r;
+  return GB_OK;
+}
+
+}  // namespace
+
+extern "C" int gb_batch_create(int count, const long long* row_off_host, const long long* nnz_off_host,
+                               const int* ia, const int* ja, const double* a, const char* prec_name,
+                               gb_batch* out) {
+  if (!out || count <= 0 || !row_off_host || !nnz_off_host || !ia || !ja || !a || !prec_name)
+    return GB_BAD_INPUT;
+  *out = nullptr;
+  const int prec = gb_prec_from_name(prec_name);
+  if (prec != GB_PREC_LINE_JACOBI && prec != GB_PREC_NONE) return GB_NOT_SUPPORTED;
+  if (row_off_host[0] != 0 || nnz_off_host[0] != 0) return GB_BAD_INPUT;
+  for (int s = 0; s < count; ++s)
+    if (row_off_host[s + 1] <= row_off_host[s] || nnz_off_host[s + 1] < nnz_off_host[s]) return GB_BAD_INPUT;
+  if (row_off_host[count] >= (1LL << 31) - 1 || nnz_off_host[count] >= (1LL << 31) - 1) return GB_NOT_SUPPORTED;
+  const int N = (int)row_off_host[count];
+  std::vector<int> hia(N + 1);
+  GB_CUDA_TRY(cudaMemcpy(hia.data(), ia, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost));
+  for (int s = 0; s <= count; ++s)
+    if (hia[row_off_host[s]] != nnz_off_host[s]) return GB_BAD_INPUT;
+  for (int i = 0; i < N; ++i)
+    if (hia[i + 1] < hia[i]) return GB_BAD_INPUT;
+  gb_batch bt = new gb_batch_s();
+  bt->count = count;
+  bt->N = N;
+  bt->jacobi = prec == GB_PREC_LINE_JACOBI;
+  bt->ia = ia;
+  bt->ja = ja;
+  bt->a = a;
+  int rc = GB_OK;
+  auto fail = [&](int e) {
+    batch_free(bt);
+    return e;
+  };
+  if (cudaStreamCreateWithFlags(&bt->s, cudaStreamNonBlocking) != cudaSuccess) return fail(GB_CUDA_ERROR);
+  bt->own_stream = true;
+  // bundles per system: <= 32 rows, <= kBundleNnz entries, a longer row alone
+  std::vector<int> bun{0}, bsys, sysb(count + 1, 0), roff(count + 1);
+  for (int s = 0; s < count; ++s) {
+    roff[s] = (int)row_off_host[s];
+    sysb[s] = (int)bsys.size();
+    int r = (int)row_off_host[s];
+    const int end = (int)row_off_host[s + 1];
+    while (r < end) {
+      const int start = r;
+      long long nz = 0;
+      if (hia[r + 1] - hia[r] > kBundleNnz) {
+        ++r;
+      } else {
+        while (r < end && r - start < kBundleRows && nz + (hia[r + 1] - hia[r]) <= kBundleNnz) {
+          nz += hia[r + 1] - hia[r];
+          ++r;
+        }
+      }
+      bun.push_back(r);
+      bsys.push_back(s);
+    }
+  }
+  roff[count] = N;
+  sysb[count] = (int)bsys.size();
+  bt->nb = (int)bsys.size();
+  int* dbun = nullptr;
+  if ((rc = bupload(bt, &dbun, bun)) != GB_OK) return fail(rc);
+  bt->bundles = dbun;
+  if ((rc = bupload(bt, &bt->bsys, bsys)) != GB_OK || (rc = bupload(bt, &bt->sys_b, sysb)) != GB_OK ||
+      (rc = batch_chunks(bt, roff)) != GB_OK || (rc = batch_buffers(bt)) != GB_OK)
+    return fail(rc);
+  // 1/diag and the FP32 values
+  const int nnz = (int)nnz_off_host[count];
+  double* dr = nullptr;
+  float* a32 = nullptr;
+  int* bad = nullptr;
+  if ((rc = balloc(bt, &dr, N)) != GB_OK || (rc = balloc(bt, &a32, nnz)) != GB_OK ||
+      (rc = balloc(bt, &bad, 1)) != GB_OK)
+    return fail(rc);
+  bt->d_r = dr;
+  bt->a32 = a32;
+  cudaMemsetAsync(bad, 0, sizeof(int), bt->s);
+  batch_diag_kernel<<<grid_chunks(bt->nc), kBatchThreads, 0, bt->s>>>(batch_args(bt, 0), dr, bad);
+  if (cast_f64_to_f32(nnz, a, a32, bt->s) != GB_OK) return fail(GB_CUDA_ERROR);
+  int hbad = 0;
+  if (cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, bt->s) != cudaSuccess ||
+      cudaStreamSynchronize(bt->s) != cudaSuccess)
+    return fail(GB_CUDA_ERROR);
+  if (hbad) return fail(GB_BAD_INPUT);  // a row without a (nonzero) diagonal
+  *out = bt;
+  return GB_OK;
+}
+
+extern "C" int gb_batch_destroy(gb_batch bt) {
+  if (!bt) return GB_BAD_INPUT;
+  cudaStreamSynchronize(bt->s);
+  batch_free(bt);
+  return GB_OK;
+}
+
+extern "C" int gb_batch_solve(gb_batch bt, const double* b, double* x, const gb_pcg_opts* opts,
+                              int* iters_host, int* flags_host, gb_pcg_result* result) {
+  if (!bt || !b || !x) return GB_BAD_INPUT;
+  return batch_solve(bt, b, x, opts, iters_host, flags_host, result);
+}
+
+// Multi-RHS on a gb_system: a shared-matrix batch kept with the system.
+namespace gb {
+void batch_release(gb_batch bt) {
+  if (bt) batch_free(bt);
+}
+}  // namespace gb
+
+extern "C" int gb_pcg_solve_multi(gb_system sys, int nrhs, const double* B, double* X,
+                                  const gb_pcg_opts* opts, int* iters_host, gb_pcg_result* result) {
+  if (!sys || nrhs <= 0 || !B || !X) return GB_BAD_INPUT;
+  if (sys->prec != GB_PREC_LINE_JACOBI && sys->prec != GB_PREC_NONE) return GB_NOT_SUPPORTED;
+  if ((long long)nrhs * sys->n >= (1LL << 31) - 1) return GB_NOT_SUPPORTED;
+  gb_batch bt = sys->multi;
+  if (!bt || bt->count != nrhs) {
+    if (bt) batch_free(bt);
+    sys->multi = nullptr;
+    bt = new gb_batch_s();
+    bt->count = nrhs;
+    bt->shared = 1;
+    bt->n1 = sys->n;
+    bt->N = nrhs * sys->n;
+    bt->jacobi = sys->prec == GB_PREC_LINE_JACOBI;
+    bt->s = sys->s;
+    bt->ia = sys->ia;
+    bt->ja = sys->ja;
+    bt->a = sys->a;
+    bt->a32 = sys->a32;
+    bt->d_r = sys->d_r;
+    bt->bundles = sys->plan.bundles;
+    bt->nb = sys->plan.nbundles;
+    std::vector<int> roff(nrhs + 1);
+    for (int s = 0; s <= nrhs; ++s) roff[s] = s * sys->n;
+    int rc = batch_chunks(bt, roff);
+    if (rc == GB_OK) rc = batch_buffers(bt);
+    if (rc != GB_OK) {
+      batch_free(bt);
+      return rc;
+    }
+    sys->multi = bt;
+  }
+  return batch_solve(bt, B, X, opts, iters_host, nullptr, result);
+}

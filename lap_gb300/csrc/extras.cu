@@ -243,18 +243,3 @@ extern "C" int gb_profile_iteration(gb_system s, const double* b, double* x, int
   return GB_OK;
 }
 
-// ------------------------------------------------------------ batching
-extern "C" int gb_batch_create(int, const long long*, const long long*, const int*, const int*,
-                               const double*, const char*, gb_batch* out) {
-  if (out) *out = nullptr;
-  return GB_NOT_SUPPORTED;
-}
-extern "C" int gb_batch_destroy(gb_batch) { return GB_NOT_SUPPORTED; }
-extern "C" int gb_batch_solve(gb_batch, const double*, double*, const gb_pcg_opts*, int*, int*,
-                              gb_pcg_result*) {
-  return GB_NOT_SUPPORTED;
-}
-extern "C" int gb_pcg_solve_multi(gb_system, int, const double*, double*, const gb_pcg_opts*, int*,
-                                  gb_pcg_result*) {
-  return GB_NOT_SUPPORTED;
-}

@@ -133,6 +133,8 @@ static void system_free(gb_system s) {
     if (lg.exec) cudaGraphExecDestroy(lg.exec);
     if (lg.graph) cudaGraphDestroy(lg.graph);
   }
+  batch_release(s->multi);
+  s->multi = nullptr;
   spmv_plan_free(&s->plan);
   tri_plan_free(&s->L);
   tri_plan_free(&s->U);

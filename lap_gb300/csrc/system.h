@@ -85,10 +85,12 @@ struct gb_system_s {
   int* err = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
+  gb_batch multi = nullptr;  // gb_pcg_solve_multi's shared-matrix batch
   gb::LoopGraph loop[3];  // [precision]
   int loop_key[3] = {-1, -1, -1};
 };
 
 namespace gb {
 int system_ensure_hist(gb_system sys, int maxit);
+void batch_release(gb_batch bt);
 }

@@ -1,0 +1,122 @@
+"""Batching through the C ABI (gb_batch_*, gb_pcg_solve_multi): every system
+of a batch must give what the single-system solver gives for it alone -- the
+same iteration count (+-1, Jacobi family) and x within 1e-7 relative -- and
+the reference's result through the oracle (x within 1e-6, iterations +-1)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a GPU", allow_module_level=True)
+
+import lap_gb300 as gb  # noqa: E402
+import oracle  # noqa: E402
+from lap_gb300 import gen  # noqa: E402
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _mixed_batch(seed=7):
+    rng = np.random.default_rng(seed)
+    mats = [gen.knn_graph(int(n), rng=rng) for n in (300, 1500, 40, 5000, 800)]
+    mats += [gen.grid2d_unit(24, seed=3)[0], gen.grid3d_lognormal(12, seed=4)[0]]
+    rhs = [rng.uniform(-1, 1, A.n) for A in mats]
+    return mats, rhs
+
+
+@pytest.mark.parametrize("prec", ["line_jacobi", "none"])
+def test_batch_matches_single_solves_and_oracle(prec):
+    mats, rhs = _mixed_batch()
+    bt = gb.Batch(mats, prec)
+    x, its, flags, r = bt.solve(dev(np.concatenate(rhs)), tol=1e-9, maxit=20000)
+    assert r["flag"] == 0 and (flags == 0).all()
+    for s, (A, b) in enumerate(zip(mats, rhs)):
+        single = gb.System.from_csr(A, prec)
+        xs, rs = single.solve(dev(b), tol=1e-9, maxit=20000)
+        single.close()
+        assert abs(int(its[s]) - rs["iters"]) <= 1, (s, its[s], rs["iters"])
+        xb = bt.split(x)[s].cpu().numpy()
+        # different reduction order than the single solver: agreement to the solve's accuracy
+        assert np.linalg.norm(xb - xs.cpu().numpy()) / np.linalg.norm(xs.cpu().numpy()) < 1e-7
+        ref = oracle.solve(A.n, A.ia, A.ja, A.a, b, prec, 1e-9, 20000)
+        assert abs(int(its[s]) - ref["iters"]) <= 1
+        assert np.linalg.norm(xb - ref["x"]) / np.linalg.norm(ref["x"]) < 1e-6
+    assert r["rel_true_res"] < 1e-8
+    bt.close()
+
+
+def test_batch_graph_eager_and_rerun_identical():
+    mats, rhs = _mixed_batch(11)
+    bt = gb.Batch(mats)
+    b = dev(np.concatenate(rhs))
+    x1, i1, _, _ = bt.solve(b, tol=1e-8, use_graph=True)
+    x2, i2, _, _ = bt.solve(b, tol=1e-8, use_graph=False)
+    x3, i3, _, _ = bt.solve(b, tol=1e-8)
+    assert (i1 == i2).all() and (i1 == i3).all()
+    assert torch.equal(x1, x2) and torch.equal(x1, x3)  # fixed-order reductions
+    bt.close()
+
+
+def test_batch_split_precision_error_vs_fp64():
+    mats, rhs = _mixed_batch(5)
+    bt = gb.Batch(mats)
+    b = dev(np.concatenate(rhs))
+    x64, i64, _, _ = bt.solve(b, tol=1e-10, maxit=20000, precision=0)
+    x32, i32, fl, r = bt.solve(b, tol=1e-10, maxit=20000, precision=2)
+    assert (fl == 0).all() and r["outer"] >= 1
+    assert r["rel_true_res"] < 1e-10 * 1.01  # x0 = 0: tol is relative to ||b|| per system
+    for s in range(bt.count):
+        a, c = bt.split(x32)[s].cpu().numpy(), bt.split(x64)[s].cpu().numpy()
+        assert np.linalg.norm(a - c) / np.linalg.norm(c) < 1e-8
+    bt.close()
+
+
+def test_batch_maxit_flags_per_system():
+    mats, rhs = _mixed_batch(2)
+    bt = gb.Batch(mats)
+    _, its, flags, r = bt.solve(dev(np.concatenate(rhs)), tol=1e-12, maxit=5)
+    assert (flags == 1).all() and (its == 6).all() and r["flag"] == 1
+    bt.close()
+
+
+def test_batch_rejects_bad_input():
+    A = gen.grid2d_unit(8, seed=1)[0]
+    with pytest.raises(gb.GbError):
+        gb.Batch([A], "ichol")  # batches run line_jacobi / none
+    # a row without its diagonal
+    ia, ja, a = A.ia.copy(), A.ja.copy(), A.a.copy()
+    row0 = slice(ia[0], ia[1])
+    a[row0][ja[row0] == 0] = 0.0
+    with pytest.raises(gb.GbError):
+        gb.Batch([gen.CSR(A.n, ia, ja, a)])
+
+
+@pytest.mark.parametrize("prec", ["line_jacobi", "none"])
+def test_multi_rhs_matches_single_solves(prec):
+    A, _ = gen.grid3d_lognormal(16, seed=1002)
+    Bm = gen.multi_rhs(A.n, 6, seed=1005)
+    sysm = gb.System.from_csr(A, prec)
+    X, its, r = gb.solve_multi(sysm, dev(Bm), tol=1e-9, maxit=20000)
+    assert r["flag"] == 0
+    for k in range(Bm.shape[0]):
+        xs, rs = sysm.solve(dev(Bm[k]), tol=1e-9, maxit=20000)
+        assert abs(int(its[k]) - rs["iters"]) <= 1
+        assert torch.linalg.norm(X[k] - xs) / torch.linalg.norm(xs) < 1e-7
+    # split precision on the same columns
+    X2, its2, r2 = gb.solve_multi(sysm, dev(Bm), tol=1e-10, maxit=20000, precision=2)
+    X64, _, _ = gb.solve_multi(sysm, dev(Bm), tol=1e-10, maxit=20000, precision=0)
+    assert r2["flag"] == 0
+    assert float(torch.linalg.norm(X2 - X64) / torch.linalg.norm(X64)) < 1e-8
+    sysm.close()
+
+
+def test_multi_rhs_unsupported_preconditioner():
+    A, b = gen.grid2d_unit(16, seed=3)
+    sysm = gb.System.from_csr(A, "ichol")
+    with pytest.raises(gb.GbError):
+        gb.solve_multi(sysm, dev(np.stack([b, b])))
+    sysm.close()
