@@ -272,6 +272,15 @@ class System:
                                     C.byref(r)), "gb_adjoint_grad")
         return lam, G, eg, r.as_dict()
 
+    def set_values(self, a) -> None:
+        """New matrix values on the same pattern (device tensor [nnz]); refactors
+        the preconditioner (gb_system_update_values)."""
+        import torch
+
+        self.a.copy_(a.to(device="cuda", dtype=torch.float64))
+        torch.cuda.synchronize()
+        check(lib().gb_system_update_values(self.h), "gb_system_update_values")
+
     def autotune(self) -> int:
         best = C.c_int()
         check(lib().gb_autotune_spmv(self.h, C.byref(best)), "gb_autotune_spmv")
