@@ -210,6 +210,162 @@ def run_kernels_only(args, local):
     print(json.dumps({"kernels_only": out, "n": A.n, "nnz": A.nnz}), flush=True)
 
 
+def _timed_solves(fn, steps):
+    import torch
+
+    out = []
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        out.append(fn())
+    return out
+
+
+def _edge_positions(A, ei, ej):
+    """CSR positions of each edge's two entries and of every diagonal, and the
+    index of each edge among A's strict-lower entries (row-major)."""
+    rows = np.repeat(np.arange(A.n), np.diff(A.ia))
+    key = rows.astype(np.int64) * A.n + A.ja
+    lo, hi = np.minimum(ei, ej), np.maximum(ei, ej)
+    strict_lower = np.nonzero(A.ja < rows)[0]
+    p_lh = np.searchsorted(key, lo * A.n + hi)
+    p_hl = np.searchsorted(key, hi * A.n + lo)
+    diag = np.searchsorted(key, np.arange(A.n, dtype=np.int64) * (A.n + 1))
+    return lo, hi, p_lh, p_hl, diag, np.searchsorted(strict_lower, p_hl)
+
+
+def run_workload(args, local):
+    """The survey's other configurations at full size (parity cases beside the
+    headline bench line): one JSON line each with times and accuracy."""
+    import torch
+
+    import lap_gb300 as gb
+    from lap_gb300 import gen
+
+    torch.cuda.set_device(local)
+    wl = args.workload
+    line = {"workload": wl, "data": "synthetic (seeded generator)"}
+    t0 = time.time()
+    if wl == "jacobi256":
+        import oracle
+
+        A, b = gen.grid2d_unit(256, seed=1001)
+        line["config"] = "256^2 unit 5-point + 1e-2 I, line_jacobi, tol 1e-8, maxit 10000 (FP64)"
+        sysm = gb.System.from_csr(A, "line_jacobi")
+        db = torch.from_numpy(b).cuda()
+        for _ in range(3):
+            sysm.solve(db, tol=1e-8, maxit=10000)
+        res = _timed_solves(lambda: sysm.solve(db, tol=1e-8, maxit=10000), 5)
+        x, r = res[-1]
+        ref = oracle.solve(A.n, A.ia, A.ja, A.a, b, "line_jacobi", 1e-8, 10000)
+        line.update(ms=statistics.mean(rr["device_ms"] for _, rr in res), iters=r["iters"],
+                    ref_iters=ref["iters"], rel_true_res=r["rel_true_res"],
+                    x_rel_err_vs_reference=float(np.linalg.norm(x.cpu().numpy() - ref["x"]) /
+                                                 np.linalg.norm(ref["x"])),
+                    cpu_reference_ms=ref["solve_s"] * 1e3, cpu_cores=1)
+    elif wl == "chunglu4m":
+        A, b = gen.chung_lu(1 << 22, seed=1003)
+        line["config"] = f"Chung-Lu n={A.n} nnz={A.nnz}, A=1.001 D - W, ichol, tol 1e-10"
+        line["generate_s"] = round(time.time() - t0, 1)
+        t1 = time.time()
+        sysm = gb.System.from_csr(A, "ichol")
+        line["setup_s"] = round(time.time() - t1, 1)
+        line["levels"] = sysm.info()
+        db = torch.from_numpy(b).cuda()
+        kw = dict(tol=1e-10, maxit=20000)
+        x64, r64 = sysm.solve(db, precision=0, **kw)
+        for p in (0, 1, 2):
+            sysm.solve(db, precision=p, **kw)
+            x, r = sysm.solve(db, precision=p, **kw)
+            line[f"precision{p}"] = {"ms": round(r["device_ms"], 2), "iters": r["iters"], "outer": r["outer"],
+                                     "flag": r["flag"], "rel_true_res": r["rel_true_res"],
+                                     "rel_err_vs_fp64": float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64))}
+    elif wl == "batch512":
+        mats, rhs = gen.knn_batch(512, seed=1004)
+        line["config"] = (f"512 kNN(k=8) Laplacians, n log-uniform 1k-200k (sum n = {sum(A.n for A in mats)}, "
+                          f"sum nnz = {sum(A.nnz for A in mats)}), line_jacobi, tol 1e-8, one graph launch")
+        line["generate_s"] = round(time.time() - t0, 1)
+        bt = gb.Batch(mats, "line_jacobi")
+        db = torch.from_numpy(np.concatenate(rhs)).cuda()
+        x64, i64, f64, r64 = bt.solve(db, tol=1e-8, maxit=20000, precision=0)
+        for p in (0, 2):
+            bt.solve(db, tol=1e-8, maxit=20000, precision=p)
+            res = _timed_solves(lambda: bt.solve(db, tol=1e-8, maxit=20000, precision=p), 3)
+            x, its, fl, r = res[-1]
+            line[f"precision{p}"] = {"ms": round(statistics.mean(rr["device_ms"] for *_, rr in res), 2),
+                                     "max_iters": int(its.max()), "all_converged": bool((fl == 0).all()),
+                                     "rel_true_res_max": r["rel_true_res"],
+                                     "rel_err_vs_fp64": float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64))}
+        t2 = time.time()  # the same systems one by one with the single-system solver
+        ms = 0.0
+        for A, b in zip(mats, rhs):
+            sg = gb.System.from_csr(A, "line_jacobi")
+            _, rs = sg.solve(torch.from_numpy(b).cuda(), tol=1e-8, maxit=20000)
+            ms += rs["device_ms"]
+            sg.close()
+        line["one_by_one_device_ms"] = round(ms, 2)
+        line["one_by_one_wall_s"] = round(time.time() - t2, 1)
+    elif wl == "multirhs32":
+        A, _ = gen.grid3d_lognormal(128, seed=1002)
+        Bm = torch.from_numpy(gen.multi_rhs(A.n, 32, seed=1005)).cuda()
+        line["config"] = "128^3 lognormal Laplacian, 32 RHS, line_jacobi, tol 1e-8, one graph launch"
+        sysm = gb.System.from_csr(A, "line_jacobi")
+        X64, i64, _ = gb.solve_multi(sysm, Bm, tol=1e-8, maxit=20000, precision=0)
+        for p in (0, 2):
+            gb.solve_multi(sysm, Bm, tol=1e-8, maxit=20000, precision=p)
+            X, its, r = gb.solve_multi(sysm, Bm, tol=1e-8, maxit=20000, precision=p)
+            line[f"precision{p}"] = {"ms": round(r["device_ms"], 2), "max_iters": int(its.max()),
+                                     "flag": r["flag"], "rel_true_res_max": r["rel_true_res"],
+                                     "rel_err_vs_fp64": float(torch.linalg.norm(X - X64) / torch.linalg.norm(X64))}
+        ms = 0.0
+        for k in range(Bm.shape[0]):
+            _, rs = sysm.solve(Bm[k], tol=1e-8, maxit=20000)
+            ms += rs["device_ms"]
+        line["one_by_one_device_ms"] = round(ms, 2)
+    elif wl == "adjoint1024":
+        nside = 1024
+        ei, ej, w = gen.grid2d_aniso_edges(nside, seed=1006)
+        A = gen.laplacian_from_edges(nside * nside, ei, ej, w, shift=1e-2)
+        rng = np.random.default_rng(1006)
+        xs = torch.from_numpy(rng.standard_normal(A.n)).cuda()
+        b = torch.from_numpy(rng.uniform(-1, 1, A.n)).cuda()
+        line["config"] = ("1024^2 anisotropic lognormal grid + 1e-2 I, ichol, loss 0.5||x-x*||^2; forward and "
+                          "adjoint in split precision (tol 1e-10); central differences h=1e-6 (FP64, tol 1e-13)")
+        sysm = gb.System.from_csr(A, "ichol")
+        kw = dict(tol=1e-10, maxit=20000, precision=2)
+        sysm.solve(b, **kw)
+        x, rf = sysm.solve(b, **kw)
+        lam, G, eg, ra = sysm.adjoint(x, (x - xs).contiguous(), **kw)
+        line["forward_ms"], line["adjoint_ms"] = round(rf["device_ms"], 2), round(ra["device_ms"], 2)
+        line["iters"] = [rf["iters"], ra["iters"]]
+        lo, hi, p_lh, p_hl, diag, t_of_edge = _edge_positions(A, ei, ej)
+        a0 = torch.from_numpy(A.a).cuda()
+        edges = np.random.default_rng(1007).choice(len(w), args.fd_edges, replace=False)
+        fds, ads = [], []
+        for e in edges:
+            vals = []
+            for sgn in (1.0, -1.0):
+                a = a0.clone()
+                d = sgn * 1e-6
+                a[int(p_lh[e])] -= d
+                a[int(p_hl[e])] -= d
+                a[int(diag[lo[e]])] += d
+                a[int(diag[hi[e]])] += d
+                sysm.set_values(a)
+                xe, _ = sysm.solve(b, tol=1e-13, maxit=50000, precision=0)
+                vals.append(0.5 * float(torch.sum((xe - xs) ** 2)))
+            fds.append((vals[0] - vals[1]) / 2e-6)
+            ads.append(float(eg[int(t_of_edge[e])]))
+        sysm.set_values(a0)
+        fds, ads = np.array(fds), np.array(ads)
+        line["fd_edges"] = int(args.fd_edges)
+        line["fd_abs_err_max_over_max_grad"] = float(np.abs(fds - ads).max() / np.abs(ads).max())
+        line["fd_rel_err_median"] = float(np.median(np.abs(fds - ads) / np.abs(ads)))
+    else:
+        raise SystemExit(f"unknown workload {wl}")
+    line["wall_s"] = round(time.time() - t0, 1)
+    print(json.dumps(line), flush=True)
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -339,6 +495,10 @@ def main():
     ap.add_argument("--kernels-only", action="store_true",
                     help="only the eager per-kernel profile of each precision mode (for ncu)")
     ap.add_argument("--profile-iters", type=int, default=3)
+    ap.add_argument("--workload", default="ichol128",
+                    choices=["ichol128", "jacobi256", "chunglu4m", "batch512", "multirhs32", "adjoint1024"],
+                    help="ichol128 is the headline line; the others are the remaining configurations")
+    ap.add_argument("--fd-edges", type=int, default=16)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_init(args)
@@ -346,6 +506,8 @@ def main():
         run_reference(args, world, rank)
     elif args.kernels_only:
         run_kernels_only(args, local)
+    elif args.workload != "ichol128":
+        run_workload(args, local)
     else:
         import __graft_entry__
 

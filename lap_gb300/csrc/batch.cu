@@ -15,7 +15,7 @@
 //   breduce_check per system: the stopping test; counts the systems still
 //                 running and ends the graph's while loop when none is
 // Reductions are segmented and in fixed order (partials per bundle / chunk,
-// summed by one warp per system), so results are reproducible.  A system
+// summed by one block per system), so results are reproducible.  A system
 // that stopped costs one flag read per bundle.  Preconditioners: line_jacobi
 // (y = D^-1 x, line_jacobi.c:3-7) and none.
 //
@@ -85,19 +85,36 @@ __device__ __forceinline__ double dr_at(const BatchArgs& B, int s, int i) {
   return B.shared ? B.d_r[i - s * B.n1] : B.d_r[i];
 }
 
-// Runs `body(s, slot, off)` for every (bundle, system) pair of this warp's
-// share: block-diagonal bundles belong to one system; a shared-matrix bundle
-// is visited once per system (its entries stay in L1 across the visits).
+// Runs `body(bundle, s, slot, off)` for every (bundle, system) pair of this
+// warp's share: a block-diagonal bundle belongs to one system; a shared-
+// matrix bundle is visited once per system, by consecutive warps (system
+// fastest), so its entries are read from HBM once and from L1 after that.
 template <typename F>
 __device__ __forceinline__ void for_bundles(const BatchArgs& B, F&& body) {
-  const int warps = gridDim.x * kBatchWarps;
-  for (int bb = blockIdx.x * kBatchWarps + (threadIdx.x >> 5); bb < B.nb; bb += warps) {
-    if (!B.shared) {
-      body(bb, B.bsys[bb], bb, 0);
-    } else {
-      for (int s = 0; s < B.count; ++s) body(bb, s, s * B.nb + bb, s * B.n1);
+  const long long warps = (long long)gridDim.x * kBatchWarps;
+  const long long w0 = (long long)blockIdx.x * kBatchWarps + (threadIdx.x >> 5);
+  if (!B.shared) {
+    for (long long bb = w0; bb < B.nb; bb += warps) body((int)bb, B.bsys[bb], (int)bb, 0);
+  } else {
+    const long long pairs = (long long)B.nb * B.count;
+    for (long long t = w0; t < pairs; t += warps) {
+      const int bb = (int)(t / B.count), s = (int)(t % B.count);
+      body(bb, s, s * B.nb + bb, s * B.n1);
     }
   }
+}
+
+// Fixed-order sum of NV interleaved partials part[stride*i + k], i in
+// [i0, i1), by the whole block; valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_segment_sum(const double* part, int stride, int i0, int i1,
+                                                  double (&v)[NV], double* sm) {
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = 0.0;
+  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] += part[(size_t)stride * i + k];
+  block_sum<NV>(v, sm);
 }
 
 // ------------------------------------------------------------ prologue
@@ -132,19 +149,14 @@ __global__ void __launch_bounds__(kBatchThreads) bresid_kernel(BatchArgs B) {
   });
 }
 
-// Per system: ||r0||, the stopping threshold, rho.
+// Per system (one block each): ||r0||, the stopping threshold, rho.
 __global__ void __launch_bounds__(kBatchThreads) breduce_init_kernel(BatchArgs B) {
-  const int lane = threadIdx.x & 31;
-  const int s = blockIdx.x * kBatchWarps + (threadIdx.x >> 5);
-  if (s >= B.count) return;
-  double v0 = 0.0, v1 = 0.0;
-  for (int i = sys_bundle_begin(B, s) + lane; i < sys_bundle_end(B, s); i += 32) {
-    v0 += B.part_b[3 * i];
-    v1 += B.part_b[3 * i + 1];
-  }
-  v0 = warp_sum(v0);
-  v1 = warp_sum(v1);
-  if (lane == 0) {
+  __shared__ double sm[2 * kBatchWarps];
+  const int s = blockIdx.x;
+  double v[2];
+  block_segment_sum<2>(B.part_b, 3, sys_bundle_begin(B, s), sys_bundle_end(B, s), v, sm);
+  const double v0 = v[0], v1 = v[1];
+  if (threadIdx.x == 0) {
     PcgState& S = B.st[s];
     const double res0 = sqrt(v0);
     S.res0 = res0;
@@ -197,16 +209,14 @@ __global__ void __launch_bounds__(kBatchThreads)
 }
 
 __global__ void __launch_bounds__(kBatchThreads) breduce_alpha_kernel(BatchArgs B) {
-  const int lane = threadIdx.x & 31;
-  const int s = blockIdx.x * kBatchWarps + (threadIdx.x >> 5);
-  if (s >= B.count) return;
+  __shared__ double sm[kBatchWarps];
+  const int s = blockIdx.x;
   PcgState& S = B.st[s];
-  if (S.done) return;
-  double v = 0.0;
-  for (int i = sys_bundle_begin(B, s) + lane; i < sys_bundle_end(B, s); i += 32) v += B.part_b[3 * i];
-  v = warp_sum(v);
-  if (lane == 0) {
-    S.pq = v;
+  if (S.done) return;  // uniform in the block
+  double v[1];
+  block_segment_sum<1>(B.part_b, 3, sys_bundle_begin(B, s), sys_bundle_end(B, s), v, sm);
+  if (threadIdx.x == 0) {
+    S.pq = v[0];
     double alpha;
     if (!pcg_alpha(&S, &alpha)) {
       S.done = 1;
@@ -244,7 +254,7 @@ __global__ void __launch_bounds__(kBatchThreads) bupdate_kernel(BatchArgs B) {
   }
 }
 
-// Counts the systems still running (lane 0 of each live system's warp);
+// Counts the systems still running (thread 0 of each live system's block);
 // the last block to finish decides whether the loop continues.
 __device__ __forceinline__ void batch_loop_decide(const BatchArgs& B, cudaGraphConditionalHandle cond,
                                                   int has_cond) {
@@ -267,22 +277,17 @@ __device__ __forceinline__ void batch_loop_decide(const BatchArgs& B, cudaGraphC
 
 __global__ void __launch_bounds__(kBatchThreads)
     breduce_check_kernel(BatchArgs B, cudaGraphConditionalHandle cond, int has_cond) {
-  const int lane = threadIdx.x & 31;
-  const int s = blockIdx.x * kBatchWarps + (threadIdx.x >> 5);
-  if (s < B.count && !B.st[s].done) {
-    PcgState& S = B.st[s];
-    double v0 = 0.0, v1 = 0.0;
-    for (int c = B.sys_c[s] + lane; c < B.sys_c[s + 1]; c += 32) {
-      v0 += B.part_c[2 * c];
-      v1 += B.part_c[2 * c + 1];
-    }
-    v0 = warp_sum(v0);
-    v1 = warp_sum(v1);
-    if (lane == 0) {
-      pcg_check(&S, v0, nullptr);  // hist_len is 0 for batch systems
+  __shared__ double sm[2 * kBatchWarps];
+  const int s = blockIdx.x;
+  PcgState& S = B.st[s];
+  if (!S.done) {  // uniform in the block
+    double v[2];
+    block_segment_sum<2>(B.part_c, 2, B.sys_c[s], B.sys_c[s + 1], v, sm);
+    if (threadIdx.x == 0) {
+      pcg_check(&S, v[0], nullptr);  // hist_len is 0 for batch systems
       if (!S.done) {
         S.rho_prev = S.rho;
-        S.rho = B.jacobi ? v1 : v0;
+        S.rho = B.jacobi ? v[1] : v[0];
         atomicAdd(&B.nactive[0], 1);
       }
     }
@@ -341,30 +346,23 @@ __global__ void __launch_bounds__(kBatchThreads) btrue_kernel(BatchArgs B, int r
 // replace = 0: stores ||b - A x|| in so.spare1 and ||b|| in so.rho.
 __global__ void __launch_bounds__(kBatchThreads)
     breduce_outer_kernel(BatchArgs B, int replace, double delta, int max_outer) {
-  const int lane = threadIdx.x & 31;
-  const int s = blockIdx.x * kBatchWarps + (threadIdx.x >> 5);
-  if (s >= B.count) return;
+  __shared__ double sm[3 * kBatchWarps];
+  const int s = blockIdx.x;
   PcgState& S = B.st[s];
   PcgState& O = B.so[s];
   if (replace && !batch_needs_check(B, s)) {
     // a recurrence that stopped on maxit or breakdown is final as it is
-    if (lane == 0 && S.done && !O.done) {
+    if (threadIdx.x == 0 && S.done && !O.done) {
       O.done = 1;
       O.flag = S.flag;
       O.status = S.status;
     }
     return;
   }
-  double v0 = 0.0, v1 = 0.0, v2 = 0.0;
-  for (int i = sys_bundle_begin(B, s) + lane; i < sys_bundle_end(B, s); i += 32) {
-    v0 += B.part_b[3 * i];
-    v1 += B.part_b[3 * i + 1];
-    v2 += B.part_b[3 * i + 2];
-  }
-  v0 = warp_sum(v0);
-  v1 = warp_sum(v1);
-  v2 = warp_sum(v2);
-  if (lane != 0) return;
+  double v[3];
+  block_segment_sum<3>(B.part_b, 3, sys_bundle_begin(B, s), sys_bundle_end(B, s), v, sm);
+  const double v0 = v[0], v1 = v[1], v2 = v[2];
+  if (threadIdx.x != 0) return;
   const double rt = sqrt(v0);
   if (!replace) {
     O.spare1 = rt;
@@ -564,12 +562,12 @@ BatchArgs batch_args(gb_batch bt, int maxit) {
 }
 
 int grid_bundles(const void* k, int nb, int count, int shared) {
-  const long long warps = (long long)nb * (shared ? 1 : 1);
+  const long long warps = (long long)nb * (shared ? count : 1);
   const long long cap = (long long)device_sm_count() * occupancy_blocks(k, kBatchThreads);
   (void)count;
   return (int)std::max(1LL, std::min(cap, (warps + kBatchWarps - 1) / kBatchWarps));
 }
-int grid_sys(int count) { return std::max(1, ceil_div(count, kBatchWarps)); }
+int grid_sys(int count) { return count; }  // one block per system
 int grid_chunks(int nc) {
   return std::max(1, std::min(nc, device_sm_count() * occupancy_blocks((const void*)bupdate_kernel, kBatchThreads)));
 }

