@@ -122,6 +122,30 @@ int deps_ichol(int n, const int* ia, const int* ja, const std::vector<int>& tpos
 // dependencies' done flags (acquire) and publishes its own (release).
 constexpr int kFactorWarps = 8;
 static_assert(32 % kFactorWarps == 0, "a group must lie inside one padded level");
+// Wall-clock limit of one wait in the factorization: a power-law graph's hub
+// rows carry tens of thousands of dependencies each and chain through one
+// another, so a row may legitimately wait seconds for a hub.  A limit set
+// with gb_debug_set_spin_budget takes precedence.
+constexpr uint64_t kFactorWaitNs = 120ull * 1000000000ull;
+
+// Acquire-poll of a done flag with the factorization's limit (all lanes poll
+// the same word); false on timeout or when another wait already failed.
+__device__ __forceinline__ bool factor_wait(const int* flag, int* err) {
+  if (ld_acquire(flag) != 0) return true;
+  const uint64_t dbg = *reinterpret_cast<const volatile unsigned long long*>(err + 2);
+  const uint64_t budget = dbg ? dbg : kFactorWaitNs;
+  const uint64_t t0 = globaltimer_ns();
+  unsigned polls = 0, ns = 32u;
+  while (true) {
+    __nanosleep(ns);
+    if (ns < kMaxSleepNs) ns <<= 1;
+    if (ld_acquire(flag) != 0) return true;
+    if ((++polls & kPollCheck) == 0u && (ld_volatile(err) != 0 || globaltimer_ns() - t0 > budget)) {
+      atomicCAS(err, 0, (int)GB_TIMEOUT);
+      return false;
+    }
+  }
+}
 
 __global__ void __launch_bounds__(kFactorWarps * 32)
     ichol_factor_kernel(int norder, const int* __restrict__ order, const int* __restrict__ ia,
@@ -142,25 +166,41 @@ __global__ void __launch_bounds__(kFactorWarps * 32)
     if (j < 0) continue;  // level padding (warp-uniform)
     const int d = dpos[j], je = ia[j + 1];
     bool ok = true;
-    for (int k = ia[j]; k < d; ++k) {  // dependencies i = ja[k] < j, ascending
-      const int i = ja[k];
-      ok = __all_sync(0xffffffffu, wait_flag(done + i, err));
-      if (!ok) break;
-      const int m = tpos[k];  // (i, j) inside row i's upper part
-      // row i was written by another SM: read it through L2 (ld.global.cg)
-      const double uij = __ldcg(f + m);
-      const int ie = ia[i + 1];
-      for (int l = m + lane; l < ie; l += 32) {
-        const int c = ja[l];
-        int lo = d, hi = je - 1;  // bisection for column c in row j's upper part
-        while (lo < hi) {
-          const int mid = (lo + hi) >> 1;
-          if (ja[mid] < c) lo = mid + 1;
-          else hi = mid;
+    // dependencies i = ja[k] < j, ascending, 32 at a time: lane t reads the
+    // done flag (acquire), u_ij and row i's end of dependency k0 + t in
+    // parallel; a dependency not finished yet is then awaited in its turn
+    for (int k0 = ia[j]; k0 < d && ok; k0 += 32) {
+      const int kl = k0 + lane;
+      const int il = kl < d ? ja[kl] : -1;
+      const int ml = kl < d ? tpos[kl] : 0;
+      const int ready_l = il < 0 ? 1 : ld_acquire(done + il);
+      const double ul = (il >= 0 && ready_l) ? __ldcg(f + ml) : 0.0;
+      const int iel = il >= 0 ? ia[il + 1] : 0;
+      __syncwarp();  // lanes' acquires order every lane's later reads of those rows
+      const int nk = min(32, d - k0);
+      for (int t = 0; t < nk; ++t) {
+        const int i = __shfl_sync(0xffffffffu, il, t);
+        const int m = __shfl_sync(0xffffffffu, ml, t);  // (i, j) inside row i's upper part
+        const int ie = __shfl_sync(0xffffffffu, iel, t);
+        double uij = __shfl_sync(0xffffffffu, ul, t);
+        if (!__shfl_sync(0xffffffffu, ready_l, t)) {
+          ok = __all_sync(0xffffffffu, factor_wait(done + i, err));
+          if (!ok) break;
+          // row i was written by another SM: read it through L2 (ld.global.cg)
+          uij = __ldcg(f + m);
         }
-        if (ja[lo] == c) f[lo] = sub_rn(f[lo], mul_rn(uij, __ldcg(f + l)));
+        for (int l = m + lane; l < ie; l += 32) {
+          const int c = ja[l];
+          int lo = d, hi = je - 1;  // bisection for column c in row j's upper part
+          while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (ja[mid] < c) lo = mid + 1;
+            else hi = mid;
+          }
+          if (ja[lo] == c) f[lo] = sub_rn(f[lo], mul_rn(uij, __ldcg(f + l)));
+        }
+        __syncwarp();  // this dependency's updates land before the next one's
       }
-      __syncwarp();  // this dependency's updates land before the next one's
     }
     if (!ok) continue;  // timed out: the row stays unpublished, dependents time out too
     const double piv = f[d];

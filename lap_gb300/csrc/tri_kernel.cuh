@@ -235,7 +235,9 @@ __device__ __forceinline__ void wait_level(const int* s_done, int need, int* err
 // of other tiles' values.  After the wait only the tile-local values are
 // read (one round of shared-memory loads) and the FMA chain runs; the
 // completion is published before the global stores.
-constexpr int kTriHeld = 4;  // dependencies held in registers per row
+constexpr int kTriHeld = 4;       // dependencies held in registers per row
+constexpr int kTriTailBatch = 8;  // loads in flight per row beyond the held ones
+constexpr int kTriLongBatch = 4;  // loads in flight per lane in a LONG record
 
 template <typename T, bool EXACT, typename OP>
 __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy, int t0, int t1,
@@ -299,11 +301,26 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
   wait_level(s_done, h.wait_for, A.err);
   T yv = T(0);
   if (lng) {
+    // lane-strided over the row; each lane issues kTriLongBatch loads before
+    // it consumes them (same per-lane order as one at a time)
     T s = T(0);
-    for (int k = lane; k < h.len; k += 32) {
-      const int c = __ldg(A.long_col + h.off + k);
-      const T v = (c >= t0 && c < t1) ? sy[c - t0] : dep_value(A, sy, c, t0, t1);
-      s = fma_rn(__ldg(A.long_val + h.off + k), v, s);
+    for (int k0 = lane; k0 < h.len; k0 += 32 * kTriLongBatch) {
+      int cb[kTriLongBatch];
+      T lb[kTriLongBatch], vb[kTriLongBatch];
+#pragma unroll
+      for (int u = 0; u < kTriLongBatch; ++u) {
+        const int k = k0 + 32 * u;
+        cb[u] = k < h.len ? __ldg(A.long_col + h.off + k) : -1;
+        lb[u] = cb[u] >= 0 ? __ldg(A.long_val + h.off + k) : T(0);
+        vb[u] = cb[u] < 0 ? T(0) : (cb[u] >= t0 && cb[u] < t1) ? sy[cb[u] - t0] : ld_relaxed(A.y + cb[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < kTriLongBatch; ++u) {
+        if (cb[u] < 0) continue;
+        T v = vb[u];
+        if ((cb[u] < t0 || cb[u] >= t1) && is_sentinel(v)) v = wait_value_slow(A.y + cb[u], A.err);
+        s = fma_rn(lb[u], v, s);
+      }
     }
     s = warp_sum(s);
     if (lane == 0) {
@@ -325,12 +342,27 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
         acc = EXACT ? sub_rn(acc, mul_rn(hl[k], v)) : fma_rn(-hl[k], v, acc);
       }
     }
-    for (int k = kTriHeld; k < h.len; ++k) {
-      const int c = cols[k * R4 + lane];
-      if (c < 0) break;
-      const T l = vals[k * R4 + lane];
-      const T v = (c >= t0 && c < t1) ? sy[c - t0] : dep_value(A, sy, c, t0, t1);
-      acc = EXACT ? sub_rn(acc, mul_rn(l, v)) : fma_rn(-l, v, acc);
+    // the rest of the row, kTriTailBatch dependencies at a time: all their
+    // loads are issued before the first is consumed (a power-law row has
+    // dozens, each an L2 round trip), then the terms are added in column
+    // order; padding columns (-1) end the row
+    for (int k0 = kTriHeld; k0 < h.len; k0 += kTriTailBatch) {
+      int cb[kTriTailBatch];
+      T lb[kTriTailBatch], vb[kTriTailBatch];
+#pragma unroll
+      for (int u = 0; u < kTriTailBatch; ++u) {
+        const int k = k0 + u;
+        cb[u] = k < h.len ? cols[k * R4 + lane] : -1;
+        lb[u] = cb[u] >= 0 ? vals[k * R4 + lane] : T(0);
+        vb[u] = cb[u] < 0 ? T(0) : (cb[u] >= t0 && cb[u] < t1) ? sy[cb[u] - t0] : ld_relaxed(A.y + cb[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < kTriTailBatch; ++u) {
+        if (cb[u] < 0) continue;
+        T v = vb[u];
+        if ((cb[u] < t0 || cb[u] >= t1) && is_sentinel(v)) v = wait_value_slow(A.y + cb[u], A.err);
+        acc = EXACT ? sub_rn(acc, mul_rn(lb[u], v)) : fma_rn(-lb[u], v, acc);
+      }
     }
     yv = publishable(EXACT ? div_rn(acc, dg) : acc);
     sy[row - t0] = yv;
