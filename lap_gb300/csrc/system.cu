@@ -274,10 +274,10 @@ extern "C" int gb_system_create(int n, int nnz, const int* ia, const int* ja, co
     }
     CK(tri_plan_build(dl, &s->L));
     CK(tri_plan_build(du, &s->U));
-    // IC(0)'s rows are cheap to start, so FP32 tiles twice as tall (half the
-    // tile-boundary crossings) pay; GS_std's backward sweep gathers a row of
-    // A per row and needs the parallelism of the FP64 tiling
-    const int t32 = prec == GB_PREC_ICHOL ? tri_default_tile_rows32(n) : tri_default_tile_rows(n);
+    // FP32 tiles as tall as the FP64 ones: that leaves shared memory for the
+    // inbox of the cluster form, whose hand-off between consecutive tiles is
+    // cheaper than taller tiles; GBLAP_TRI_TILE_ROWS32 sets them explicitly
+    const int t32 = getenv("GBLAP_TRI_TILE_ROWS32") ? tri_default_tile_rows32(n) : tri_default_tile_rows(n);
     CK(tri_plan_build(dl, &s->L32, t32));
     CK(tri_plan_build(du, &s->U32, t32));
   }

@@ -239,9 +239,42 @@ constexpr int kTriHeld = 4;       // dependencies held in registers per row
 constexpr int kTriTailBatch = 8;  // loads in flight per row beyond the held ones
 constexpr int kTriLongBatch = 4;  // loads in flight per lane in a LONG record
 
+// Link of a tile to its neighbours inside a thread-block cluster: `in` is
+// this CTA's inbox (shared memory) holding the previous tile's rows
+// [in0, in1), pushed there by the CTA that solves them; `out` is the
+// shared::cluster address of the next CTA's inbox (0: none).  Without a
+// cluster both are empty and every other-tile value comes through L2.
+template <typename T>
+struct TriLink {
+  const T* in = nullptr;
+  int in0 = 0, in1 = 0;
+  uint32_t out = 0;
+};
+
+__device__ __forceinline__ void st_cluster(uint32_t addr, float v) {
+  asm volatile("st.relaxed.cluster.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
+}
+__device__ __forceinline__ void st_cluster(uint32_t addr, double v) {
+  asm volatile("st.relaxed.cluster.shared::cluster.f64 [%0], %1;" ::"r"(addr), "d"(v) : "memory");
+}
+
+// A value of another tile: from the inbox when the previous tile pushes it
+// there, else from global memory (sentinel while not yet solved).
+template <typename T>
+__device__ __forceinline__ T other_tile_read(const TriArgs<T>& A, const TriLink<T>& L, int c) {
+  if (L.in && c >= L.in0 && c < L.in1) return *(const volatile T*)(L.in + (c - L.in0));
+  return ld_relaxed(A.y + c);
+}
+template <typename T>
+__device__ __forceinline__ T other_tile_wait(const TriArgs<T>& A, const TriLink<T>& L, int c) {
+  if (L.in && c >= L.in0 && c < L.in1) return wait_local_slow(L.in + (c - L.in0), A.err);
+  return wait_value_slow(A.y + c, A.err);
+}
+
 template <typename T, bool EXACT, typename OP>
 __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy, int t0, int t1,
-                                             const unsigned char* rec, int lane, int* s_done) {
+                                             const unsigned char* rec, int lane, int* s_done,
+                                             const TriLink<T>& L) {
   const RecHdr h = *reinterpret_cast<const RecHdr*>(rec);
   const int R4 = (h.nrows + 3) & ~3;
   const int* rows = reinterpret_cast<const int*>(rec + sizeof(RecHdr));
@@ -271,7 +304,7 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
       hc[k] = c;
       if (c >= 0) {
         hl[k] = vals[k * R4 + lane];
-        if (c < t0 || c >= t1) hv[k] = ld_relaxed(A.y + c);  // other tile: read early
+        if (c < t0 || c >= t1) hv[k] = other_tile_read(A, L, c);  // other tile: read early
       }
     }
   }
@@ -292,7 +325,7 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
 #pragma unroll
     for (int k = 0; k < kTriHeld; ++k) {
       if (pend[k] && (hc[k] < t0 || hc[k] >= t1)) {
-        const T v = is_sentinel(hv[k]) ? wait_value_slow(A.y + hc[k], A.err) : hv[k];
+        const T v = is_sentinel(hv[k]) ? other_tile_wait(A, L, hc[k]) : hv[k];
         acc = fma_rn(-hl[k], v, acc);
         pend[k] = false;
       }
@@ -312,13 +345,13 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
         const int k = k0 + 32 * u;
         cb[u] = k < h.len ? __ldg(A.long_col + h.off + k) : -1;
         lb[u] = cb[u] >= 0 ? __ldg(A.long_val + h.off + k) : T(0);
-        vb[u] = cb[u] < 0 ? T(0) : (cb[u] >= t0 && cb[u] < t1) ? sy[cb[u] - t0] : ld_relaxed(A.y + cb[u]);
+        vb[u] = cb[u] < 0 ? T(0) : (cb[u] >= t0 && cb[u] < t1) ? sy[cb[u] - t0] : other_tile_read(A, L, cb[u]);
       }
 #pragma unroll
       for (int u = 0; u < kTriLongBatch; ++u) {
         if (cb[u] < 0) continue;
         T v = vb[u];
-        if ((cb[u] < t0 || cb[u] >= t1) && is_sentinel(v)) v = wait_value_slow(A.y + cb[u], A.err);
+        if ((cb[u] < t0 || cb[u] >= t1) && is_sentinel(v)) v = other_tile_wait(A, L, cb[u]);
         s = fma_rn(lb[u], v, s);
       }
     }
@@ -338,7 +371,7 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
     for (int k = 0; k < kTriHeld; ++k) {
       if (pend[k]) {
         T v = hv[k];
-        if (is_sentinel(v)) v = wait_value_slow(A.y + hc[k], A.err);  // other tile, not yet written
+        if (is_sentinel(v)) v = other_tile_wait(A, L, hc[k]);  // other tile, not yet written
         acc = EXACT ? sub_rn(acc, mul_rn(hl[k], v)) : fma_rn(-hl[k], v, acc);
       }
     }
@@ -354,13 +387,13 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
         const int k = k0 + u;
         cb[u] = k < h.len ? cols[k * R4 + lane] : -1;
         lb[u] = cb[u] >= 0 ? vals[k * R4 + lane] : T(0);
-        vb[u] = cb[u] < 0 ? T(0) : (cb[u] >= t0 && cb[u] < t1) ? sy[cb[u] - t0] : ld_relaxed(A.y + cb[u]);
+        vb[u] = cb[u] < 0 ? T(0) : (cb[u] >= t0 && cb[u] < t1) ? sy[cb[u] - t0] : other_tile_read(A, L, cb[u]);
       }
 #pragma unroll
       for (int u = 0; u < kTriTailBatch; ++u) {
         if (cb[u] < 0) continue;
         T v = vb[u];
-        if ((cb[u] < t0 || cb[u] >= t1) && is_sentinel(v)) v = wait_value_slow(A.y + cb[u], A.err);
+        if ((cb[u] < t0 || cb[u] >= t1) && is_sentinel(v)) v = other_tile_wait(A, L, cb[u]);
         acc = EXACT ? sub_rn(acc, mul_rn(lb[u], v)) : fma_rn(-lb[u], v, acc);
       }
     }
@@ -370,27 +403,73 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
   __syncwarp();
   if (lane == 0) red_release_cta_add(s_done, 1);
   if (act && (!lng || lane == 0)) {
+    if (L.out) st_cluster(L.out + (uint32_t)(row - t0) * (uint32_t)sizeof(T), yv);  // next tile's inbox
     st_relaxed(A.y + row, yv);
     op.done(row, yv, dp);
   }
 }
 
-template <typename T, typename OP, bool EXACT>
+// ------------------------------------------------------------ clusters
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// Every thread of every CTA of the cluster: release before, acquire after.
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+// shared::cluster address of `p` (a shared-memory object of this CTA) in the
+// CTA of the given rank
+__device__ __forceinline__ uint32_t cluster_map(const void* p, unsigned rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ int ld_cluster_s32(uint32_t addr) {
+  int v;
+  asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+  return v;
+}
+
+// CL = 1: one CTA per tile, tiles by ticket, every other-tile value through
+// L2.  CL > 1 (FP32): a thread-block cluster of CL CTAs takes CL consecutive
+// tiles (one group) per ticket, CTA rank r solving tile CL*g + r; each CTA
+// keeps an inbox of the previous tile's values in its shared memory, which
+// that tile's CTA fills with distributed-shared-memory stores as it solves
+// rows, so the dependency that crosses a tile boundary inside the group
+// costs a shared-memory poll instead of an L2 round trip.  Cluster barriers
+// per group: after the group is known, after every inbox holds the
+// sentinel (before any push), and at the end (no CTA refills or frees its
+// inbox while its predecessor may still push into it).
+template <typename T, typename OP, bool EXACT, int CL = 1>
 __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArgs<T> A, OP op) {
   constexpr int kTriConsumers = TriCons<T>::n;
   constexpr int kTriThreads = TriCons<T>::threads;
   extern __shared__ __align__(128) unsigned char tri_smem[];
   unsigned char* ring = tri_smem;                                     // kTriSlots x kTriSlotBytes
   T* sy = reinterpret_cast<T*>(tri_smem + kTriSlots * kTriSlotBytes);  // tile solution
+  T* inbox = sy + A.tile_rows;  // CL > 1: the previous tile's values
   __shared__ __align__(8) uint64_t full_bar[kTriSlots], empty_bar[kTriSlots];
   __shared__ long long s_roff[kTriRecTable];
   __shared__ int s_rbytes[kTriRecTable];
   __shared__ unsigned s_last_u[kTriSlots];  // last record (stream index) copied into each slot
   __shared__ int s_tile;
   __shared__ int s_done;  // records of the current tile completed
+  __shared__ int s_group;
   __shared__ double s_red[64];
   op.begin();
-  if (!op.active()) {
+  bool act = op.active();
+  if constexpr (CL > 1) {
+    // the whole cluster follows rank 0's reading, so that all its CTAs take
+    // part in the same cluster barriers (the state can only change once the
+    // last tile is done, when no tile is left for anyone to take)
+    if (cluster_rank() == 0 && threadIdx.x == 0) s_group = act ? 1 : 0;
+    cluster_sync_all();
+    act = ld_cluster_s32(cluster_map(&s_group, 0)) != 0;
+    cluster_sync_all();  // s_group is reused for the group tickets
+  }
+  if (!act) {
     if (blockIdx.x == 0 && threadIdx.x == 0) op.inactive_end();
     return;  // no ticket touched
   }
@@ -408,68 +487,93 @@ __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArg
   unsigned base = 0;       // records of earlier tiles streamed by this CTA
   bool failed = false;
   while (true) {
-    if (threadIdx.x == 0) s_tile = (int)atomicAdd(&A.ticket[0], 1u);
-    __syncthreads();
-    const int k = s_tile;
-    __syncthreads();
-    if (k >= A.ntiles) break;
-    const int t0 = __ldg(A.tile_row0 + k), t1 = __ldg(A.tile_row1 + k);
-    const int rec0 = __ldg(A.tile_rec + k), rec1 = __ldg(A.tile_rec + k + 1);
-    const int nrec = rec1 - rec0;
-    for (int q = threadIdx.x; q < nrec && q < kTriRecTable; q += kTriThreads) {
-      s_roff[q] = __ldg(A.rec_off + rec0 + q);
-      s_rbytes[q] = __ldg(A.rec_bytes + rec0 + q);
+    int k;
+    TriLink<T> link;
+    if constexpr (CL > 1) {
+      const unsigned rank = cluster_rank();
+      if (rank == 0 && threadIdx.x == 0) s_group = (int)atomicAdd(&A.ticket[0], 1u);
+      cluster_sync_all();
+      if (threadIdx.x == 0) s_tile = ld_cluster_s32(cluster_map(&s_group, 0));
+      __syncthreads();
+      const int g = s_tile;
+      if ((long long)g * CL >= A.ntiles) break;  // the same for the whole cluster
+      k = g * CL + (int)rank;                    // >= ntiles: idle in this group
+      if (k < A.ntiles && rank > 0) {
+        link.in = inbox;
+        link.in0 = __ldg(A.tile_row0 + k - 1);
+        link.in1 = __ldg(A.tile_row1 + k - 1);
+        for (int i = threadIdx.x; i < link.in1 - link.in0; i += kTriThreads) inbox[i] = sentinel<T>();
+      }
+      if (k + 1 < A.ntiles && rank + 1 < (unsigned)CL) link.out = cluster_map(inbox, rank + 1);
+      __syncthreads();
+      cluster_sync_all();  // every inbox holds the sentinel before any push
+    } else {
+      if (threadIdx.x == 0) s_tile = (int)atomicAdd(&A.ticket[0], 1u);
+      __syncthreads();
+      k = s_tile;
+      __syncthreads();
+      if (k >= A.ntiles) break;
     }
-    for (int i = threadIdx.x; i < t1 - t0; i += kTriThreads) sy[i] = sentinel<T>();
-    if (threadIdx.x == 0) s_done = 0;
-    __syncthreads();
-    if (producer) {
-      // lane j streams records j, j+L, j+2L, ... (L = kTriProdLanes): the
-      // issue of a bulk copy costs about an L2 round trip, so one lane alone
-      // would deliver records slower than the consumers solve them.  Slot
-      // u % kTriSlots is refilled by the lane that filled it before.
-      if (lane < kTriProdLanes) {
-        for (int q = lane, n = 1; q < nrec && !failed; q += kTriProdLanes, ++n) {
+    if (k < A.ntiles) {
+      const int t0 = __ldg(A.tile_row0 + k), t1 = __ldg(A.tile_row1 + k);
+      const int rec0 = __ldg(A.tile_rec + k), rec1 = __ldg(A.tile_rec + k + 1);
+      const int nrec = rec1 - rec0;
+      for (int q = threadIdx.x; q < nrec && q < kTriRecTable; q += kTriThreads) {
+        s_roff[q] = __ldg(A.rec_off + rec0 + q);
+        s_rbytes[q] = __ldg(A.rec_bytes + rec0 + q);
+      }
+      for (int i = threadIdx.x; i < t1 - t0; i += kTriThreads) sy[i] = sentinel<T>();
+      if (threadIdx.x == 0) s_done = 0;
+      __syncthreads();
+      if (producer) {
+        // lane j streams records j, j+L, j+2L, ... (L = kTriProdLanes): the
+        // issue of a bulk copy costs about an L2 round trip, so one lane alone
+        // would deliver records slower than the consumers solve them.  Slot
+        // u % kTriSlots is refilled by the lane that filled it before.
+        if (lane < kTriProdLanes) {
+          for (int q = lane, n = 1; q < nrec && !failed; q += kTriProdLanes, ++n) {
+            const unsigned u = base + q;
+            const int slot = u % kTriSlots;
+            if ((n & 15) == 0 && ld_volatile(A.err) != 0) {
+              failed = true;
+              break;
+            }
+            if (!mbar_wait(&empty_bar[slot], ((u / kTriSlots) & 1u) ^ 1u, A.err)) {
+              failed = true;
+              break;
+            }
+            const unsigned bytes = (unsigned)(q < kTriRecTable ? s_rbytes[q] : __ldg(A.rec_bytes + rec0 + q));
+            const long long off = q < kTriRecTable ? s_roff[q] : __ldg(A.rec_off + rec0 + q);
+            mbar_expect_tx(&full_bar[slot], bytes);
+            tma_load_1d(ring + slot * kTriSlotBytes, A.recbuf + off, bytes, &full_bar[slot]);
+            s_last_u[slot] = u;
+            // after the first record is on its way: warm L2 with the vectors
+            // this tile's rows read (HBM latency off the records' path)
+            if (n == 1) op.prefetch(t0, t1, lane);
+            // warm L2 with a record further ahead, so ring copies hit L2
+            const int qa = q + kTriL2Ahead;
+            if (qa < nrec && qa < kTriRecTable) tma_prefetch_l2(A.recbuf + s_roff[qa], (unsigned)s_rbytes[qa]);
+          }
+        }
+        __syncwarp();
+      } else {
+        for (int q = wid; q < nrec; q += kTriConsumers) {
           const unsigned u = base + q;
           const int slot = u % kTriSlots;
-          if ((n & 15) == 0 && ld_volatile(A.err) != 0) {
-            failed = true;
-            break;
-          }
-          if (!mbar_wait(&empty_bar[slot], ((u / kTriSlots) & 1u) ^ 1u, A.err)) {
-            failed = true;
-            break;
-          }
-          const unsigned bytes = (unsigned)(q < kTriRecTable ? s_rbytes[q] : __ldg(A.rec_bytes + rec0 + q));
-          const long long off = q < kTriRecTable ? s_roff[q] : __ldg(A.rec_off + rec0 + q);
-          mbar_expect_tx(&full_bar[slot], bytes);
-          tma_load_1d(ring + slot * kTriSlotBytes, A.recbuf + off, bytes, &full_bar[slot]);
-          s_last_u[slot] = u;
-          // after the first record is on its way: warm L2 with the vectors
-          // this tile's rows read (HBM latency off the records' path)
-          if (n == 1) op.prefetch(t0, t1, lane);
-          // warm L2 with a record further ahead, so ring copies hit L2
-          const int qa = q + kTriL2Ahead;
-          if (qa < nrec && qa < kTriRecTable) tma_prefetch_l2(A.recbuf + s_roff[qa], (unsigned)s_rbytes[qa]);
+          if (!failed && !mbar_wait(&full_bar[slot], (u / kTriSlots) & 1u, A.err)) failed = true;
+          if (!failed) solve_record<T, EXACT>(A, op, sy, t0, t1, ring + slot * kTriSlotBytes, lane, &s_done, link);
+          __syncwarp();
+          // after a failure the slot is not released: its copy may still be in
+          // flight, and the producer must not aim another copy at it
+          if (lane == 0 && !failed) mbar_arrive(&empty_bar[slot]);
         }
       }
-      __syncwarp();
-    } else {
-      for (int q = wid; q < nrec; q += kTriConsumers) {
-        const unsigned u = base + q;
-        const int slot = u % kTriSlots;
-        if (!failed && !mbar_wait(&full_bar[slot], (u / kTriSlots) & 1u, A.err)) failed = true;
-        if (!failed) solve_record<T, EXACT>(A, op, sy, t0, t1, ring + slot * kTriSlotBytes, lane, &s_done);
-        __syncwarp();
-        // after a failure the slot is not released: its copy may still be in
-        // flight, and the producer must not aim another copy at it
-        if (lane == 0 && !failed) mbar_arrive(&empty_bar[slot]);
-      }
+      base += nrec;
+      __syncthreads();
+      op.chunk_end(k, A.ntiles, A.ticket, s_red);
+      __syncthreads();
     }
-    base += nrec;
-    __syncthreads();
-    op.chunk_end(k, A.ntiles, A.ticket, s_red);
-    __syncthreads();
+    if constexpr (CL > 1) cluster_sync_all();  // the group's pushes are complete
   }
   // Drain: every issued copy must have landed before the CTA's shared
   // memory goes away.  A slot is refilled only after its previous record was
@@ -502,37 +606,76 @@ __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArg
 }
 
 int tri_blocks_per_sm();
+bool tri_cluster_enabled();
+
+constexpr int kTriCluster = 8;  // CTAs (consecutive tiles) per cluster for FP32 solves
+
+template <typename T, typename OP, bool EXACT, int CL>
+int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, size_t smem) {
+  auto kern = tri_tile_kernel<T, OP, EXACT, CL>;
+  static bool attr_set = false;  // one per instantiation
+  if (!attr_set) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kTriMaxDynSmem));
+    attr_set = true;
+  }
+  if constexpr (CL > 1) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(TriCons<T>::threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const int groups = (p.ntiles + CL - 1) / CL;
+    cfg.gridDim = dim3(groups * CL);
+    int active = 0;
+    if (cudaOccupancyMaxActiveClusters(&active, kern, &cfg) != cudaSuccess || active < 1) {
+      cudaGetLastError();
+      return GB_NOT_SUPPORTED;
+    }
+    cfg.gridDim = dim3((groups < active ? groups : active) * CL);
+    GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, A, op));
+    return GB_OK;
+  } else {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TriCons<T>::threads, smem) != cudaSuccess ||
+        per_sm < 1) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
+    per_sm = per_sm < tri_blocks_per_sm() ? per_sm : tri_blocks_per_sm();
+    const long long cap = (long long)device_sm_count() * per_sm;
+    const int grid = (int)(p.ntiles < cap ? p.ntiles : cap);
+    kern<<<grid, TriCons<T>::threads, smem, s>>>(A, op);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+  }
+}
 
 // Launches the tiled solve: dynamic shared memory = the record ring plus one
-// tile of T values; a persistent grid of min(tiles, SMs x resident CTAs).
+// tile of T values (plus the inbox tile in the cluster form).  FP32 tiles
+// that fit with an inbox run in clusters of kTriCluster when the device can
+// hold such a cluster; everything else runs the per-CTA form on a persistent
+// grid of min(tiles, SMs x resident CTAs).
 template <typename T, typename OP, bool EXACT>
 int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   if (p.ntiles <= 0) return GB_OK;
   const size_t smem = (size_t)kTriSlots * kTriSlotBytes + (size_t)p.tile_rows * sizeof(T);
   if (smem > (size_t)kTriMaxDynSmem) return GB_NOT_SUPPORTED;  // an FP32-only plan in FP64
-  static bool attr_set = false;  // one per instantiation
-  if (!attr_set) {
-    GB_CUDA_TRY(cudaFuncSetAttribute(tri_tile_kernel<T, OP, EXACT>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kTriMaxDynSmem));
-    attr_set = true;
+  if constexpr (sizeof(T) == 4) {
+    const size_t smem_cl = smem + (size_t)p.tile_rows * sizeof(T);
+    if (p.ntiles > 1 && smem_cl <= (size_t)kTriMaxDynSmem && tri_cluster_enabled()) {
+      const int rc = tri_launch_cl<T, OP, EXACT, kTriCluster>(p, A, op, s, smem_cl);
+      if (rc != GB_NOT_SUPPORTED) return rc;
+    }
   }
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tri_tile_kernel<T, OP, EXACT>,
-                                                    TriCons<T>::threads, smem) != cudaSuccess ||
-      per_sm < 1) {
-    cudaGetLastError();
-    per_sm = 1;
-  }
-  per_sm = per_sm < tri_blocks_per_sm() ? per_sm : tri_blocks_per_sm();
-  const long long cap = (long long)device_sm_count() * per_sm;
-  const int grid = (int)(p.ntiles < cap ? p.ntiles : cap);
-  tri_tile_kernel<T, OP, EXACT><<<grid, TriCons<T>::threads, smem, s>>>(A, op);
-  GB_CUDA_TRY(cudaGetLastError());
-  return GB_OK;
+  return tri_launch_cl<T, OP, EXACT, 1>(p, A, op, s, smem);
 }
 
-// fma_form: FP64 solves read the FMA-form records (the PCG); FP32 solves
-// always do.  The exact (EXACT) solves pass false.
 template <typename T>
 TriArgs<T> tri_args(const TriPlan& p, T* y, int* err, bool fma_form);
 

@@ -387,6 +387,17 @@ int tri_blocks_per_sm() {
 
 void tri_set_blocks_per_sm(int bps) { g_tri_bps = std::max(1, std::min(8, bps)); }
 
+// FP32 solves in thread-block clusters (distributed-shared-memory hand-off
+// between consecutive tiles); GBLAP_TRI_CLUSTER=0 selects the per-CTA form.
+bool tri_cluster_enabled() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("GBLAP_TRI_CLUSTER");
+    v = (e && e[0] == '0') ? 0 : 1;
+  }
+  return v == 1;
+}
+
 int tri_grid(int ntiles) {
   return std::max(1, std::min(ntiles, device_sm_count() * tri_blocks_per_sm()));
 }
