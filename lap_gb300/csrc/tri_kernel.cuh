@@ -606,12 +606,16 @@ __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArg
 }
 
 int tri_blocks_per_sm();
-bool tri_cluster_enabled();
+// CTAs per cluster for FP32 solves: -1 automatic (8 or 4), 0 per-CTA form,
+// 4 or 8 forced (GBLAP_TRI_CLUSTER)
+int tri_cluster_size();
 
-constexpr int kTriCluster = 8;  // CTAs (consecutive tiles) per cluster for FP32 solves
-
+// need_all: refuse (GB_NOT_SUPPORTED) unless every group of tiles gets a
+// cluster at once -- a group left for later starts only when a whole cluster
+// has finished, after the pipeline it belongs to has moved on
 template <typename T, typename OP, bool EXACT, int CL>
-int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, size_t smem) {
+int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, size_t smem,
+                  bool need_all = false) {
   auto kern = tri_tile_kernel<T, OP, EXACT, CL>;
   static bool attr_set = false;  // one per instantiation
   if (!attr_set) {
@@ -637,6 +641,7 @@ int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, 
       cudaGetLastError();
       return GB_NOT_SUPPORTED;
     }
+    if (need_all && active < groups) return GB_NOT_SUPPORTED;
     cfg.gridDim = dim3((groups < active ? groups : active) * CL);
     GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, A, op));
     return GB_OK;
@@ -658,9 +663,10 @@ int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, 
 
 // Launches the tiled solve: dynamic shared memory = the record ring plus one
 // tile of T values (plus the inbox tile in the cluster form).  FP32 tiles
-// that fit with an inbox run in clusters of kTriCluster when the device can
-// hold such a cluster; everything else runs the per-CTA form on a persistent
-// grid of min(tiles, SMs x resident CTAs).
+// that fit with an inbox run in clusters: of 8 CTAs when all groups of 8
+// tiles fit the device at once, else of 4 when those do, else of 8;
+// everything else runs the per-CTA form on a persistent grid of
+// min(tiles, SMs x resident CTAs).
 template <typename T, typename OP, bool EXACT>
 int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   if (p.ntiles <= 0) return GB_OK;
@@ -668,8 +674,16 @@ int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   if (smem > (size_t)kTriMaxDynSmem) return GB_NOT_SUPPORTED;  // an FP32-only plan in FP64
   if constexpr (sizeof(T) == 4) {
     const size_t smem_cl = smem + (size_t)p.tile_rows * sizeof(T);
-    if (p.ntiles > 1 && smem_cl <= (size_t)kTriMaxDynSmem && tri_cluster_enabled()) {
-      const int rc = tri_launch_cl<T, OP, EXACT, kTriCluster>(p, A, op, s, smem_cl);
+    const int want = tri_cluster_size();
+    if (p.ntiles > 1 && smem_cl <= (size_t)kTriMaxDynSmem && want != 0) {
+      int rc = GB_NOT_SUPPORTED;
+      if (want == 8) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
+      else if (want == 4) rc = tri_launch_cl<T, OP, EXACT, 4>(p, A, op, s, smem_cl);
+      else {
+        rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl, true);
+        if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 4>(p, A, op, s, smem_cl, true);
+        if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
+      }
       if (rc != GB_NOT_SUPPORTED) return rc;
     }
   }

@@ -388,14 +388,16 @@ int tri_blocks_per_sm() {
 void tri_set_blocks_per_sm(int bps) { g_tri_bps = std::max(1, std::min(8, bps)); }
 
 // FP32 solves in thread-block clusters (distributed-shared-memory hand-off
-// between consecutive tiles); GBLAP_TRI_CLUSTER=0 selects the per-CTA form.
-bool tri_cluster_enabled() {
-  static int v = -1;
-  if (v < 0) {
+// between consecutive tiles): GBLAP_TRI_CLUSTER=0 selects the per-CTA form,
+// 4 or 8 a cluster size; unset, the launcher chooses.
+int tri_cluster_size() {
+  static int v = -2;
+  if (v == -2) {
     const char* e = getenv("GBLAP_TRI_CLUSTER");
-    v = (e && e[0] == '0') ? 0 : 1;
+    const int x = e ? atoi(e) : -1;
+    v = (x == 0 || x == 4 || x == 8) ? x : -1;
   }
-  return v == 1;
+  return v;
 }
 
 int tri_grid(int ntiles) {
