@@ -663,10 +663,12 @@ int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, 
 
 // Launches the tiled solve: dynamic shared memory = the record ring plus one
 // tile of T values (plus the inbox tile in the cluster form).  FP32 tiles
-// that fit with an inbox run in clusters: of 8 CTAs when all groups of 8
-// tiles fit the device at once, else of 4 when those do, else of 8;
-// everything else runs the per-CTA form on a persistent grid of
-// min(tiles, SMs x resident CTAs).
+// that fit with an inbox run in clusters of 8 CTAs (4 where 8 cannot be
+// placed).  On 128^3 (128 tiles) only 15 clusters of 8 fit at once, so the
+// last group starts late, and still 8 beats all-resident clusters of 4: a
+// tile boundary inside a cluster costs a shared-memory poll, one between
+// clusters an L2 round trip.  Everything else runs the per-CTA form on a
+// persistent grid of min(tiles, SMs x resident CTAs).
 template <typename T, typename OP, bool EXACT>
 int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   if (p.ntiles <= 0) return GB_OK;
@@ -680,9 +682,8 @@ int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
       if (want == 8) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
       else if (want == 4) rc = tri_launch_cl<T, OP, EXACT, 4>(p, A, op, s, smem_cl);
       else {
-        rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl, true);
-        if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 4>(p, A, op, s, smem_cl, true);
-        if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
+        rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
+        if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 4>(p, A, op, s, smem_cl);
       }
       if (rc != GB_NOT_SUPPORTED) return rc;
     }
