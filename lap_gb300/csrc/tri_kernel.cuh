@@ -610,12 +610,9 @@ int tri_blocks_per_sm();
 // 4 or 8 forced (GBLAP_TRI_CLUSTER)
 int tri_cluster_size();
 
-// need_all: refuse (GB_NOT_SUPPORTED) unless every group of tiles gets a
-// cluster at once -- a group left for later starts only when a whole cluster
-// has finished, after the pipeline it belongs to has moved on
+// GB_NOT_SUPPORTED when the device cannot place one cluster of CL CTAs.
 template <typename T, typename OP, bool EXACT, int CL>
-int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, size_t smem,
-                  bool need_all = false) {
+int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, size_t smem) {
   auto kern = tri_tile_kernel<T, OP, EXACT, CL>;
   static bool attr_set = false;  // one per instantiation
   if (!attr_set) {
@@ -641,7 +638,6 @@ int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, 
       cudaGetLastError();
       return GB_NOT_SUPPORTED;
     }
-    if (need_all && active < groups) return GB_NOT_SUPPORTED;
     cfg.gridDim = dim3((groups < active ? groups : active) * CL);
     GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, A, op));
     return GB_OK;
