@@ -208,16 +208,17 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// rho = r'w after a composed preconditioner (PREC kind)
-template <typename T>
+// rho = r'w after a composed preconditioner (PREC kind), and after the
+// split recurrence's FP32 upper solve (FP64 r, FP32 w): rho_prev <- rho.
+template <typename T, typename TW = T>
 __global__ void __launch_bounds__(kThreads)
-    rho_kernel(int n, const T* __restrict__ r, const T* __restrict__ w, PcgState* st,
+    rho_kernel(int n, const T* __restrict__ r, const TW* __restrict__ w, PcgState* st,
                double* part) {
   __shared__ double sm[kThreads / 32];
   if (st->done) return;
   double acc[1] = {0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    acc[0] += (double)r[i] * (double)w[i];
+    acc[0] = fma((double)r[i], (double)w[i], acc[0]);
   if (reduce_last<1>(acc, part, gridDim.x, blockIdx.x, &st->tk[TK_RHO], sm) && threadIdx.x == 0) {
     st->rho_prev = st->rho;
     st->rho = acc[0];
@@ -374,6 +375,9 @@ struct OpIcUpper {
 // y = (D+U)^-1 rhs, w = t + y (GS.c:40), reducing r'w.
 template <typename T, typename TR = T>
 struct OpGsUpper {
+  // each row gathers a row of A before its solve: a group of tiles left for
+  // later costs a whole slow tile, so all cluster groups should fit at once
+  static constexpr bool kPreferResident = true;
   const T* t;
   const TR* r;
   const int* ia;
@@ -444,6 +448,34 @@ struct OpSplitLower {
   }
   __device__ void prefetch(int r0, int r1, int part) const {
     prefetch_rows_l2(r, r0, r1, part, kTriProdLanes);
+  }
+  __device__ void chunk_end(int, int nchunks, unsigned* ticket, double*) {
+    if (threadIdx.x == 0) chunk_finished(ticket, nchunks);
+  }
+};
+
+// IC(0) upper solve of the split recurrence: y = U^{-1} t only.  r'w is
+// reduced right after by rho_kernel, a bandwidth pass (FP64 r, FP32 w), so
+// that no FP64 arithmetic queues on GB300's narrow FP64 pipe in front of
+// the solve's dependency chain.
+template <typename T>
+struct OpSplitUpper {
+  const T* t;
+  PcgState* st;
+  bool dn;
+  __device__ void begin() { dn = st->done != 0; }
+  __device__ bool active() const { return !dn; }
+  __device__ void inactive_end() {}
+  struct Pre {
+    T t;
+  };
+  struct DPre {};
+  __device__ Pre pre(int i) const { return {t[i]}; }
+  __device__ T rhs(int, const Pre& v) const { return v.t; }
+  __device__ DPre dpre(int) const { return {}; }
+  __device__ void done(int, T, const DPre&) {}
+  __device__ void prefetch(int r0, int r1, int part) const {
+    prefetch_rows_l2(t, r0, r1, part, kTriProdLanes);
   }
   __device__ void chunk_end(int, int nchunks, unsigned* ticket, double*) {
     if (threadIdx.x == 0) chunk_finished(ticket, nchunks);
@@ -748,9 +780,13 @@ static int launch_lower_split(gb_system sys, PcgState* st) {
 
 static int launch_upper_split(gb_system sys, PcgState* st) {
   if (sys->prec == GB_PREC_ICHOL) {
-    OpIcUpper<float, double> op{sys->v32.t, sys->v64.r, st, sys->part, false, 0.0};
-    return tri_launch<float, OpIcUpper<float, double>, false>(
-        sys->U32, tri_args<float>(sys->U32, sys->v32.s, sys->err, true), op, sys->s);
+    OpSplitUpper<float> op{sys->v32.t, st, false};
+    GB_TRY((tri_launch<float, OpSplitUpper<float>, false>(
+        sys->U32, tri_args<float>(sys->U32, sys->v32.s, sys->err, true), op, sys->s)));
+    rho_kernel<double, float><<<grid_ew(sys->n), kThreads, 0, sys->s>>>(sys->n, sys->v64.r, sys->v32.s,
+                                                                        st, sys->part);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
   }
   OpGsUpper<float, double> op{sys->v32.t, sys->v64.r, sys->ia, sys->ja, sys->a32, sys->v32.w,
                               st, sys->part, false, 0.0};
