@@ -482,6 +482,62 @@ struct OpSplitUpper {
   }
 };
 
+// GS_std (k = 1) backward sweep of the split recurrence, with its right-hand
+// side g = r - A t computed beforehand by gs_rhs_split_kernel: y = (D+U)^{-1}
+// g, w = t + y (GS.c:40); r'w is reduced afterwards by rho_kernel.
+template <typename T>
+struct OpSplitGsUpper {
+  const T* g;
+  const T* t;
+  T* w;
+  PcgState* st;
+  bool dn;
+  __device__ void begin() { dn = st->done != 0; }
+  __device__ bool active() const { return !dn; }
+  __device__ void inactive_end() {}
+  struct Pre {
+    T g;
+  };
+  struct DPre {
+    T t;
+  };
+  __device__ Pre pre(int i) const { return {g[i]}; }
+  __device__ T rhs(int, const Pre& v) const { return v.g; }
+  __device__ DPre dpre(int i) const { return {t[i]}; }
+  __device__ void done(int i, T y, const DPre& v) { w[i] = v.t + y; }
+  __device__ void prefetch(int r0, int r1, int part) const {
+    prefetch_rows_l2(g, r0, r1, part, kTriProdLanes);
+    prefetch_rows_l2(t, r0, r1, part, kTriProdLanes);
+  }
+  __device__ void chunk_end(int, int nchunks, unsigned* ticket, double*) {
+    if (threadIdx.x == 0) chunk_finished(ticket, nchunks);
+  }
+};
+
+// g = r - A t in FP32 (GS.c:34-35), as a bandwidth pass over A before the
+// backward sweep.  Each row runs the same FMA chain OpGsUpper runs inside
+// its solve, negated: fma(-a, t, acc) = -fma(a, t, -acc) exactly, so the
+// row-bundle SpMV computes -(r - A t) starting from -r, bit for bit (rows of
+// more than kBundleNnz entries are summed by the whole warp instead).
+__global__ void __launch_bounds__(kThreads)
+    gs_rhs_split_kernel(int n, int nb, const int* __restrict__ bundles, const int* __restrict__ ia,
+                        const int* __restrict__ ja, const float* __restrict__ a,
+                        const float* __restrict__ t, const double* __restrict__ r, float* g,
+                        const PcgState* st) {
+  __shared__ float stage[kThreads / 32][kBundleNnz];
+  if (st->done) return;
+  XPlain<float> xf{t};
+  struct Ep {
+    const double* r;
+    float* g;
+    __device__ float init(int i) const { return -(float)r[i]; }
+    __device__ void store(int i, float v) { g[i] = -v; }
+  } ep{r, g};
+  const int wid = threadIdx.x >> 5;
+  for (int bb = blockIdx.x * (kThreads / 32) + wid; bb < nb; bb += gridDim.x * (kThreads / 32))
+    spmv_bundle<float, false>(bb, n, bundles, ia, ja, a, 1.0f, xf, ep, stage[wid]);
+}
+
 // ------------------------------------------------------------ spmv_pq (split)
 // Split precision: q = A w + beta q and p = w + beta p with w the FP32 output
 // of the preconditioner, A's FP32 values and FP32 products (A w), and p, q,
@@ -788,10 +844,20 @@ static int launch_upper_split(gb_system sys, PcgState* st) {
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
   }
-  OpGsUpper<float, double> op{sys->v32.t, sys->v64.r, sys->ia, sys->ja, sys->a32, sys->v32.w,
-                              st, sys->part, false, 0.0};
-  return tri_launch<float, OpGsUpper<float, double>, false>(
-      sys->U32, tri_args<float>(sys->U32, sys->v32.s, sys->err, true), op, sys->s);
+  // GS_std: g = r - A t (v32.r holds g; the split recurrence keeps r in FP64),
+  // the sweep, then r'w
+  const int nb = sys->plan.nbundles;
+  gs_rhs_split_kernel<<<wave_grid(gs_rhs_split_kernel, kThreads, ceil_div(nb, kThreads / 32)), kThreads, 0,
+                        sys->s>>>(sys->n, nb, sys->plan.bundles, sys->ia, sys->ja, sys->a32, sys->v32.t,
+                                  sys->v64.r, sys->v32.r, st);
+  GB_CUDA_TRY(cudaGetLastError());
+  OpSplitGsUpper<float> op{sys->v32.r, sys->v32.t, sys->v32.w, st, false};
+  GB_TRY((tri_launch<float, OpSplitGsUpper<float>, false>(
+      sys->U32, tri_args<float>(sys->U32, sys->v32.s, sys->err, true), op, sys->s)));
+  rho_kernel<double, float><<<grid_ew(sys->n), kThreads, 0, sys->s>>>(sys->n, sys->v64.r, sys->v32.w, st,
+                                                                      sys->part);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
 }
 
 static int grid_split(int nb) {
