@@ -225,208 +225,15 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// ------------------------------------------------------------ fused tri ops
-// Lower solve with the x/r update fused in front (do_update): the update of
-// row i is elementwise and row i's right-hand side is r_i only, so it runs in
-// the tile-wide phase A of the solve.
-template <typename T>
-struct OpPcgLower {
-  T *x, *r;
-  const T *p, *q;
-  T* sfill;
-  PcgState* st;
-  double* part;
-  double* hist;
-  cudaGraphConditionalHandle cond;
-  int has_cond, do_update;
-  // per thread
-  bool dn, ok;
-  T a, na;
-  double rr;
-  __device__ void begin() {
-    dn = st->done != 0;
-    ok = true;
-    rr = 0.0;
-    if (do_update && !dn) {
-      double alpha;
-      ok = pcg_alpha(st, &alpha);
-      a = (T)alpha;
-      na = (T)(-alpha);
-    }
-  }
-  __device__ bool active() const { return !dn && ok; }
-  // converged before this body (dn) or breakdown (!ok): end the loop
-  __device__ void inactive_end() {
-    if (!do_update) return;
-    if (!dn && !ok) {
-      st->done = 1;
-      st->flag = 2;
-      st->status = GB_BREAKDOWN;
-    }
-    set_cond(cond, has_cond, false);
-  }
-  struct Pre {
-    T x, p, r, q;
-  };
-  struct DPre {};
-  __device__ Pre pre(int i) const {
-    if (!do_update) return {T(0), T(0), r[i], T(0)};
-    return {x[i], p[i], r[i], q[i]};
-  }
-  __device__ T rhs(int i, const Pre& v) {
-    if (!do_update) return v.r;
-    x[i] = fma_rn(a, v.p, v.x);
-    const T ri = fma_rn(na, v.q, v.r);
-    r[i] = ri;
-    rr += (double)ri * (double)ri;
-    return ri;
-  }
-  __device__ DPre dpre(int) const { return {}; }
-  __device__ void done(int i, T, const DPre&) {
-    if (sfill) sfill[i] = sentinel<T>();
-  }
-  __device__ void prefetch(int r0, int r1, int part) const {
-    prefetch_rows_l2(r, r0, r1, part, kTriProdLanes);
-    if (!do_update) return;
-    prefetch_rows_l2(x, r0, r1, part, kTriProdLanes);
-    prefetch_rows_l2(p, r0, r1, part, kTriProdLanes);
-    prefetch_rows_l2(q, r0, r1, part, kTriProdLanes);
-  }
-  __device__ void chunk_end(int c, int nchunks, unsigned* ticket, double* sm) {
-    double v[1] = {rr};
-    rr = 0.0;
-    block_sum<1>(v, sm);
-    __shared__ bool last;
-    if (threadIdx.x == 0) {
-      part[c] = v[0];
-      last = chunk_finished(ticket, nchunks);
-    }
-    __syncthreads();
-    if (!last || !do_update) return;
-    double t[1] = {0.0};
-    for (int i = threadIdx.x; i < nchunks; i += blockDim.x) t[0] += ld_relaxed(part + i);
-    block_sum<1>(t, sm);
-    if (threadIdx.x == 0) {
-      pcg_check(st, t[0], hist);
-      set_cond(cond, has_cond, !st->done && st->body_count++ < st->maxit + 4);
-    }
-  }
-};
+// ------------------------------------------------------------ tri ops
+// The PCG's triangular solves carry no FP64 vector work (GB300 issues FP64
+// at 1/64 of the FP32 rate, and anything queued on that pipe sits in front
+// of the solve's dependency chain): the x / r update runs before the lower
+// solve (update_kernel), r'w after the upper (rho_kernel), and GS_std's
+// right-hand side r - A t before its backward sweep (gs_rhs_kernel).
 
-// Shared tail of the upper-solve ops: per-tile r'w partials; the finisher
-// of the last tile rolls rho.
-__device__ __forceinline__ void rho_chunk_end(double& rho, PcgState* st, double* part, int c,
-                                              int nchunks, unsigned* ticket, double* sm) {
-  double v[1] = {rho};
-  rho = 0.0;
-  block_sum<1>(v, sm);
-  __shared__ bool last;
-  if (threadIdx.x == 0) {
-    part[c] = v[0];
-    last = chunk_finished(ticket, nchunks);
-  }
-  __syncthreads();
-  if (!last) return;
-  double s[1] = {0.0};
-  for (int i = threadIdx.x; i < nchunks; i += blockDim.x) s[0] += ld_relaxed(part + i);
-  block_sum<1>(s, sm);
-  if (threadIdx.x == 0) {
-    st->rho_prev = st->rho;
-    st->rho = s[0];
-  }
-}
-
-// Upper solve whose output is w (ichol: w = (L L^T)^-1 r), reducing r'w.
-// TR: type of the residual r (FP64 when only the solve runs in FP32).
-template <typename T, typename TR = T>
-struct OpIcUpper {
-  const T* t;
-  const TR* r;
-  PcgState* st;
-  double* part;
-  bool dn;
-  double rho;
-  __device__ void begin() {
-    dn = st->done != 0;
-    rho = 0.0;
-  }
-  __device__ bool active() const { return !dn; }
-  __device__ void inactive_end() {}
-  struct Pre {
-    T t;
-  };
-  struct DPre {
-    TR r;
-  };
-  __device__ Pre pre(int i) const { return {t[i]}; }
-  __device__ T rhs(int, const Pre& v) const { return v.t; }
-  __device__ DPre dpre(int i) const { return {r[i]}; }
-  __device__ void done(int, T y, const DPre& v) { rho += (double)v.r * (double)y; }
-  __device__ void prefetch(int r0, int r1, int part) const {
-    prefetch_rows_l2(t, r0, r1, part, kTriProdLanes);
-    prefetch_rows_l2(r, r0, r1, part, kTriProdLanes);
-  }
-  __device__ void chunk_end(int c, int nchunks, unsigned* ticket, double* sm) {
-    rho_chunk_end(rho, st, part, c, nchunks, ticket, sm);
-  }
-};
-
-// GS_std (k = 1) backward sweep: rhs_i = r_i - (A t)_i (GS.c:34-35),
-// y = (D+U)^-1 rhs, w = t + y (GS.c:40), reducing r'w.
-template <typename T, typename TR = T>
-struct OpGsUpper {
-  // each row gathers a row of A before its solve: a group of tiles left for
-  // later costs a whole slow tile, so all cluster groups should fit at once
-  static constexpr bool kPreferResident = true;
-  const T* t;
-  const TR* r;
-  const int* ia;
-  const int* ja;
-  const T* av;
-  T* w;
-  PcgState* st;
-  double* part;
-  bool dn;
-  double rho;
-  __device__ void begin() {
-    dn = st->done != 0;
-    rho = 0.0;
-  }
-  __device__ bool active() const { return !dn; }
-  __device__ void inactive_end() {}
-  struct Pre {
-    TR r;
-    int j0, j1;
-  };
-  struct DPre {
-    T t;
-    TR r;
-  };
-  __device__ Pre pre(int i) const { return {r[i], ia[i], ia[i + 1]}; }
-  __device__ T rhs(int, const Pre& v) const {
-    T acc = (T)v.r;
-    for (int j = v.j0; j < v.j1; ++j) acc = fma_rn(-av[j], t[ja[j]], acc);
-    return acc;
-  }
-  __device__ DPre dpre(int i) const { return {t[i], r[i]}; }
-  __device__ void done(int i, T y, const DPre& v) {
-    const T wi = v.t + y;
-    w[i] = wi;
-    rho += (double)v.r * (double)wi;
-  }
-  __device__ void prefetch(int r0, int r1, int part) const {
-    prefetch_rows_l2(t, r0, r1, part, kTriProdLanes);
-    prefetch_rows_l2(r, r0, r1, part, kTriProdLanes);
-    prefetch_rows_l2(ia, r0, r1, part, kTriProdLanes);
-  }
-  __device__ void chunk_end(int c, int nchunks, unsigned* ticket, double* sm) {
-    rho_chunk_end(rho, st, part, c, nchunks, ticket, sm);
-  }
-};
-
-// Lower solve of the split-precision recurrence: the FP64 residual r is the
-// right-hand side, rounded to the solve's type; the x / r update ran in the
-// FP64 update kernel before it.
+// Lower solve: the residual r is the right-hand side (rounded to the solve's
+// type in the split recurrence); also pre-fills the upper solve's output.
 template <typename T, typename TR>
 struct OpSplitLower {
   const TR* r;
@@ -454,10 +261,7 @@ struct OpSplitLower {
   }
 };
 
-// IC(0) upper solve of the split recurrence: y = U^{-1} t only.  r'w is
-// reduced right after by rho_kernel, a bandwidth pass (FP64 r, FP32 w), so
-// that no FP64 arithmetic queues on GB300's narrow FP64 pipe in front of
-// the solve's dependency chain.
+// IC(0) upper solve: y = U^{-1} t only; r'w follows in rho_kernel.
 template <typename T>
 struct OpSplitUpper {
   const T* t;
@@ -482,9 +286,9 @@ struct OpSplitUpper {
   }
 };
 
-// GS_std (k = 1) backward sweep of the split recurrence, with its right-hand
-// side g = r - A t computed beforehand by gs_rhs_split_kernel: y = (D+U)^{-1}
-// g, w = t + y (GS.c:40); r'w is reduced afterwards by rho_kernel.
+// GS_std (k = 1) backward sweep, with its right-hand side g = r - A t
+// computed beforehand by gs_rhs_kernel: y = (D+U)^{-1} g, w = t + y
+// (GS.c:34-40); r'w follows in rho_kernel.
 template <typename T>
 struct OpSplitGsUpper {
   const T* g;
@@ -514,28 +318,28 @@ struct OpSplitGsUpper {
   }
 };
 
-// g = r - A t in FP32 (GS.c:34-35), as a bandwidth pass over A before the
-// backward sweep.  Each row runs the same FMA chain OpGsUpper runs inside
-// its solve, negated: fma(-a, t, acc) = -fma(a, t, -acc) exactly, so the
-// row-bundle SpMV computes -(r - A t) starting from -r, bit for bit (rows of
-// more than kBundleNnz entries are summed by the whole warp instead).
+// g = r - A t (GS.c:34-35) in the solve's type T, as a bandwidth pass over
+// A before the backward sweep: acc = r; acc = fma(-a_ij, t_j, acc) along
+// the row.  fma(-a, t, acc) = -fma(a, t, -acc) exactly, so the row-bundle
+// SpMV computes that chain negated, starting from -r (rows of more than
+// kBundleNnz entries are summed by the whole warp instead).
+template <typename T, typename TR>
 __global__ void __launch_bounds__(kThreads)
-    gs_rhs_split_kernel(int n, int nb, const int* __restrict__ bundles, const int* __restrict__ ia,
-                        const int* __restrict__ ja, const float* __restrict__ a,
-                        const float* __restrict__ t, const double* __restrict__ r, float* g,
-                        const PcgState* st) {
-  __shared__ float stage[kThreads / 32][kBundleNnz];
+    gs_rhs_kernel(int n, int nb, const int* __restrict__ bundles, const int* __restrict__ ia,
+                  const int* __restrict__ ja, const T* __restrict__ a, const T* __restrict__ t,
+                  const TR* __restrict__ r, T* g, const PcgState* st) {
+  __shared__ T stage[kThreads / 32][kBundleNnz];
   if (st->done) return;
-  XPlain<float> xf{t};
+  XPlain<T> xf{t};
   struct Ep {
-    const double* r;
-    float* g;
-    __device__ float init(int i) const { return -(float)r[i]; }
-    __device__ void store(int i, float v) { g[i] = -v; }
+    const TR* r;
+    T* g;
+    __device__ T init(int i) const { return -(T)r[i]; }
+    __device__ void store(int i, T v) { g[i] = -v; }
   } ep{r, g};
   const int wid = threadIdx.x >> 5;
   for (int bb = blockIdx.x * (kThreads / 32) + wid; bb < nb; bb += gridDim.x * (kThreads / 32))
-    spmv_bundle<float, false>(bb, n, bundles, ia, ja, a, 1.0f, xf, ep, stage[wid]);
+    spmv_bundle<T, false>(bb, n, bundles, ia, ja, a, T(1), xf, ep, stage[wid]);
 }
 
 // ------------------------------------------------------------ spmv_pq (split)
@@ -748,37 +552,44 @@ bool prec_fused_tri(int prec, int k) {
   return prec == GB_PREC_ICHOL || (prec == GB_PREC_GS_STD && k == 1);
 }
 
-// Launches the fused lower solve (prologue: do_update = 0).
+// The lower solve; with do_update, preceded by the x / r update and the
+// stopping test (update_kernel, which also ends the graph's loop).
 template <typename T>
 static int launch_lower(gb_system sys, PcgState* st, int do_update, cudaGraphConditionalHandle cond,
                         int has_cond) {
   auto v = vecs<T>(sys);
-  OpPcgLower<T> op{};
-  op.x = v.x;
-  op.r = v.r;
-  op.p = v.p0;
-  op.q = v.q;
-  op.sfill = v.s;
-  op.st = st;
-  op.part = sys->part;
-  op.hist = sys->hist;
-  op.cond = cond;
-  op.has_cond = has_cond;
-  op.do_update = do_update;
+  if (do_update) {
+    update_kernel<T, WK_PREC><<<grid_ew(sys->n), kThreads, 0, sys->s>>>(
+        sys->n, v.x, v.r, nullptr, v.p0, v.q, nullptr, st, sys->part, sys->hist, cond, has_cond);
+    GB_CUDA_TRY(cudaGetLastError());
+  }
   const TriPlan& L = sizeof(T) == 8 ? sys->L : sys->L32;
-  return tri_launch<T, OpPcgLower<T>, false>(L, tri_args<T>(L, v.t, sys->err, true), op, sys->s);
+  OpSplitLower<T, T> op{v.r, v.s, st, false};
+  return tri_launch<T, OpSplitLower<T, T>, false>(L, tri_args<T>(L, v.t, sys->err, true), op, sys->s);
 }
 
+// The upper solve and r'w (GS_std: g = r - A t first; p1 holds g).
 template <typename T>
 static int launch_upper(gb_system sys, PcgState* st) {
   auto v = vecs<T>(sys);
   const TriPlan& U = sizeof(T) == 8 ? sys->U : sys->U32;
   if (sys->prec == GB_PREC_ICHOL) {
-    OpIcUpper<T> op{v.t, v.r, st, sys->part, false, 0.0};
-    return tri_launch<T, OpIcUpper<T>, false>(U, tri_args<T>(U, v.s, sys->err, true), op, sys->s);
+    OpSplitUpper<T> op{v.t, st, false};
+    GB_TRY((tri_launch<T, OpSplitUpper<T>, false>(U, tri_args<T>(U, v.s, sys->err, true), op, sys->s)));
+    rho_kernel<T><<<grid_ew(sys->n), kThreads, 0, sys->s>>>(sys->n, v.r, v.s, st, sys->part);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
   }
-  OpGsUpper<T> op{v.t, v.r, sys->ia, sys->ja, mat_vals<T>(sys), v.w, st, sys->part, false, 0.0};
-  return tri_launch<T, OpGsUpper<T>, false>(U, tri_args<T>(U, v.s, sys->err, true), op, sys->s);
+  const int nb = sys->plan.nbundles;
+  gs_rhs_kernel<T, T><<<wave_grid(gs_rhs_kernel<T, T>, kThreads, ceil_div(nb, kThreads / 32)), kThreads, 0,
+                        sys->s>>>(sys->n, nb, sys->plan.bundles, sys->ia, sys->ja, mat_vals<T>(sys), v.t, v.r,
+                                  v.p1, st);
+  GB_CUDA_TRY(cudaGetLastError());
+  OpSplitGsUpper<T> op{v.p1, v.t, v.w, st, false};
+  GB_TRY((tri_launch<T, OpSplitGsUpper<T>, false>(U, tri_args<T>(U, v.s, sys->err, true), op, sys->s)));
+  rho_kernel<T><<<grid_ew(sys->n), kThreads, 0, sys->s>>>(sys->n, v.r, v.w, st, sys->part);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
 }
 
 // w buffer the spmv_pq kernel gathers: ichol's w is the upper solve's output
@@ -847,9 +658,9 @@ static int launch_upper_split(gb_system sys, PcgState* st) {
   // GS_std: g = r - A t (v32.r holds g; the split recurrence keeps r in FP64),
   // the sweep, then r'w
   const int nb = sys->plan.nbundles;
-  gs_rhs_split_kernel<<<wave_grid(gs_rhs_split_kernel, kThreads, ceil_div(nb, kThreads / 32)), kThreads, 0,
-                        sys->s>>>(sys->n, nb, sys->plan.bundles, sys->ia, sys->ja, sys->a32, sys->v32.t,
-                                  sys->v64.r, sys->v32.r, st);
+  gs_rhs_kernel<float, double><<<wave_grid(gs_rhs_kernel<float, double>, kThreads, ceil_div(nb, kThreads / 32)),
+                                 kThreads, 0, sys->s>>>(sys->n, nb, sys->plan.bundles, sys->ia, sys->ja,
+                                                        sys->a32, sys->v32.t, sys->v64.r, sys->v32.r, st);
   GB_CUDA_TRY(cudaGetLastError());
   OpSplitGsUpper<float> op{sys->v32.r, sys->v32.t, sys->v32.w, st, false};
   GB_TRY((tri_launch<float, OpSplitGsUpper<float>, false>(

@@ -31,7 +31,7 @@
 // waiters release their dependents with a NaN and the CTA drains its own
 // copies before leaving.
 //
-// OP contract (fused vector updates and dot products of the PCG):
+// OP contract (right-hand side and epilogue of each solved row):
 //   void begin();  bool active();  void inactive_end()   (block 0, !active)
 //   Pre pre(int row)                loads of the rhs (issued early)
 //   T rhs(int row, const Pre&)      rhs value (may store updated vectors)
@@ -610,11 +610,9 @@ int tri_blocks_per_sm();
 // 4 or 8 forced (GBLAP_TRI_CLUSTER)
 int tri_cluster_size();
 
-// GB_NOT_SUPPORTED when the device cannot place one cluster of CL CTAs, or,
-// with need_all, cannot place every group's cluster at once.
+// GB_NOT_SUPPORTED when the device cannot place one cluster of CL CTAs.
 template <typename T, typename OP, bool EXACT, int CL>
-int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, size_t smem,
-                  bool need_all = false) {
+int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, size_t smem) {
   auto kern = tri_tile_kernel<T, OP, EXACT, CL>;
   static bool attr_set = false;  // one per instantiation
   if (!attr_set) {
@@ -640,7 +638,6 @@ int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, 
       cudaGetLastError();
       return GB_NOT_SUPPORTED;
     }
-    if (need_all && active < groups) return GB_NOT_SUPPORTED;
     cfg.gridDim = dim3((groups < active ? groups : active) * CL);
     GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, A, op));
     return GB_OK;
@@ -660,17 +657,6 @@ int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, 
   }
 }
 
-// Ops whose rows do heavy work before their solve (OP::kPreferResident)
-// want every cluster group placed at once.
-template <typename OP, typename = void>
-struct TriPrefersResident {
-  static constexpr bool value = false;
-};
-template <typename OP>
-struct TriPrefersResident<OP, decltype((void)OP::kPreferResident)> {
-  static constexpr bool value = OP::kPreferResident;
-};
-
 // Launches the tiled solve: dynamic shared memory = the record ring plus one
 // tile of T values (plus the inbox tile in the cluster form).  FP32 tiles
 // that fit with an inbox run in clusters of 8 CTAs (4 where 8 cannot be
@@ -678,7 +664,6 @@ struct TriPrefersResident<OP, decltype((void)OP::kPreferResident)> {
 // last group starts late, and still 8 beats all-resident clusters of 4 for
 // the IC(0) solves (188 vs 201 ms per PCG solve): a tile boundary inside a
 // cluster costs a shared-memory poll, one between clusters an L2 round trip.
-// Ops with heavy rows prefer sizes whose groups all fit (8, then 4).
 // Everything else runs the per-CTA form on a persistent grid of
 // min(tiles, SMs x resident CTAs).
 template <typename T, typename OP, bool EXACT>
@@ -694,11 +679,7 @@ int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
       if (want == 8) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
       else if (want == 4) rc = tri_launch_cl<T, OP, EXACT, 4>(p, A, op, s, smem_cl);
       else {
-        if (TriPrefersResident<OP>::value) {
-          rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl, true);
-          if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 4>(p, A, op, s, smem_cl, true);
-        }
-        if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
+        rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
         if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 4>(p, A, op, s, smem_cl);
       }
       if (rc != GB_NOT_SUPPORTED) return rc;
