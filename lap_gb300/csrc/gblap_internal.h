@@ -33,7 +33,7 @@ namespace gb {
 constexpr int kBundleRows = 32;   // rows per SpMV bundle (one warp)
 constexpr int kBundleNnz = 512;   // products staged per bundle (4 KB FP64)
 constexpr int kSpmvWarps = 8;     // warps per SpMV block
-constexpr int kRedBlocksPerSM = 8;
+constexpr int kRedBlocksPerSM = 4;
 constexpr int kRedThreads = 256;
 
 // ----------------------------------------------------------- SpMV plan

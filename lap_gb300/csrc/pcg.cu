@@ -145,23 +145,17 @@ __global__ void __launch_bounds__(kThreads)
     T beta;
     bool first;
     double pq;
-    T wv, pv, qv;  // the row's operands, loaded by pre()
     __device__ T init(int) const { return T(0); }
-    __device__ void pre(int i) {
-      wv = w[i];
-      pv = first ? T(0) : p[i];
-      qv = first ? T(0) : q[i];
-    }
     __device__ void store(int i, T s) {
-      const T wi = wv;
-      const T pi = first ? wi : fma_rn(beta, pv, wi);
-      const T qi = first ? s : fma_rn(beta, qv, s);
+      const T wi = w[i];
+      const T pi = first ? wi : fma_rn(beta, p[i], wi);
+      const T qi = first ? s : fma_rn(beta, q[i], s);
       p[i] = pi;
       q[i] = qi;
       pq += (double)pi * (double)qi;
       if (tf) tf[i] = sentinel<T>();
     }
-  } ep{w, p, q, tfill, beta, first, 0.0, T(0), T(0), T(0)};
+  } ep{w, p, q, tfill, beta, first, 0.0};
   const int wid = threadIdx.x >> 5;
   for (int bb = blockIdx.x * (kThreads / 32) + wid; bb < nb; bb += gridDim.x * (kThreads / 32))
     spmv_bundle<T, false>(bb, n, bundles, ia, ja, a, T(1), xf, ep, stage[wid]);
@@ -173,10 +167,9 @@ __global__ void __launch_bounds__(kThreads)
 // ------------------------------------------------------------ update
 template <typename T, int WK>
 __global__ void __launch_bounds__(kThreads)
-    update_kernel(int n, T* __restrict__ x, T* __restrict__ r, T* __restrict__ w,
-                  const T* __restrict__ p, const T* __restrict__ q, const T* __restrict__ d_r,
-                  PcgState* st, double* part, double* hist, cudaGraphConditionalHandle cond,
-                  int has_cond) {
+    update_kernel(int n, T* x, T* r, T* w, const T* __restrict__ p, const T* __restrict__ q,
+                  const T* __restrict__ d_r, PcgState* st, double* part, double* hist,
+                  cudaGraphConditionalHandle cond, int has_cond) {
   __shared__ double sm[2 * kThreads / 32];
   if (st->done) {
     if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(cond, has_cond, false);
@@ -194,9 +187,9 @@ __global__ void __launch_bounds__(kThreads)
   }
   const T al = (T)alpha, nal = (T)(-alpha);
   double acc[2] = {0.0, 0.0};
-  auto row = [&](int i, T xi, T pi, T ri0, T qi) {
-    x[i] = fma_rn(al, pi, xi);
-    const T ri = fma_rn(nal, qi, ri0);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] = fma_rn(al, p[i], x[i]);
+    const T ri = fma_rn(nal, q[i], r[i]);
     r[i] = ri;
     acc[0] += (double)ri * (double)ri;
     if (WK == WK_JACOBI) {
@@ -204,25 +197,7 @@ __global__ void __launch_bounds__(kThreads)
       w[i] = wi;
       acc[1] += (double)ri * (double)wi;
     }
-  };
-  // four rows per thread per step, their loads issued before any use (the
-  // kernel is bound by loads in flight); same per-thread order as one by one
-  const int stride = gridDim.x * blockDim.x;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i + 3 * stride < n; i += 4 * stride) {
-    T xv[4], pv[4], rv[4], qv[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int k = i + u * stride;
-      xv[u] = x[k];
-      pv[u] = p[k];
-      rv[u] = r[k];
-      qv[u] = q[k];
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) row(i + u * stride, xv[u], pv[u], rv[u], qv[u]);
   }
-  for (; i < n; i += stride) row(i, x[i], p[i], r[i], q[i]);
   if (reduce_last<2>(acc, part, gridDim.x, blockIdx.x, &st->tk[TK_UPD], sm) && threadIdx.x == 0) {
     pcg_check(st, acc[0], hist);
     if (WK != WK_PREC) {
@@ -393,24 +368,17 @@ __global__ void __launch_bounds__(kThreads)
     double beta;
     bool first;
     double pq;
-    float wv;
-    double pv, qv;  // the row's operands, loaded by pre()
     __device__ float init(int) const { return 0.0f; }
-    __device__ void pre(int i) {
-      wv = w[i];
-      pv = first ? 0.0 : p[i];
-      qv = first ? 0.0 : q[i];
-    }
     __device__ void store(int i, float s) {
-      const double wi = (double)wv;
-      const double pi = first ? wi : fma_rn(beta, pv, wi);
-      const double qi = first ? (double)s : fma_rn(beta, qv, (double)s);
+      const double wi = (double)w[i];
+      const double pi = first ? wi : fma_rn(beta, p[i], wi);
+      const double qi = first ? (double)s : fma_rn(beta, q[i], (double)s);
       p[i] = pi;
       q[i] = qi;
       pq = fma_rn(pi, qi, pq);
       if (tf) tf[i] = sentinel<float>();
     }
-  } ep{w, p, q, tfill, beta, first, 0.0, 0.0f, 0.0, 0.0};
+  } ep{w, p, q, tfill, beta, first, 0.0};
   const int wid = threadIdx.x >> 5;
   for (int bb = blockIdx.x * (kThreads / 32) + wid; bb < nb; bb += gridDim.x * (kThreads / 32))
     spmv_bundle<float, false>(bb, n, bundles, ia, ja, a, 1.0f, xf, ep, stage[wid]);

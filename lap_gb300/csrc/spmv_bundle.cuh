@@ -19,9 +19,6 @@
 // fuse their vector updates and dot products into the SpMV.
 #pragma once
 
-#include <type_traits>
-#include <utility>
-
 #include "gb_common.cuh"
 
 namespace gb {
@@ -38,20 +35,12 @@ __device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fm
 // Epilogue contract:
 //   T init(int row)           -> starting value of the row sum (beta*y or 0)
 //   void store(int row, T v)  -> consume the finished row value
-//   void pre(int row)         -> optional: issue the loads store() will need;
-//                                called for the lane's row when the bundle
-//                                starts, so they overlap the matrix traffic
 // X contract:
 //   T operator()(int col)     -> x value at col
 //
 // bundles == nullptr selects the plan-free layout: bundle b is rows
 // [32b, 32b+32); one whose entries overflow the staging buffer is walked row
 // by row with the whole warp.
-template <typename EP, typename = void>
-struct EpHasPre : std::false_type {};
-template <typename EP>
-struct EpHasPre<EP, decltype(std::declval<EP&>().pre(0))> : std::true_type {};
-
 template <typename T, bool EXACT, typename XF, typename EP>
 __device__ __forceinline__ void spmv_bundle(int b, int n, const int* __restrict__ bundles,
                                             const int* __restrict__ ia,
@@ -77,16 +66,10 @@ __device__ __forceinline__ void spmv_bundle(int b, int n, const int* __restrict_
         s = EXACT ? add_rn(s, mul_rn(mul_rn(alpha, __ldg(a + j)), xv)) : fma_rn(__ldg(a + j), xv, s);
       }
       s = warp_sum(s);
-      if (lane == 0) {
-        if constexpr (EpHasPre<EP>::value) ep.pre(r);
-        ep.store(r, add_rn(ep.init(r), s));
-      }
+      if (lane == 0) ep.store(r, add_rn(ep.init(r), s));
     }
     __syncwarp();
     return;
-  }
-  if constexpr (EpHasPre<EP>::value) {
-    if (r0 + lane < r1) ep.pre(r0 + lane);
   }
   // staging, 4 entries per lane in flight: all index/value loads of a group
   // are issued before its x gathers, which are issued before any use
