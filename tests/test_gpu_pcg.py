@@ -295,3 +295,42 @@ def test_large_grid3d_properties():
         res[prec] = r["iters"]
         sysm.close()
     assert res["ichol"] < res["line_jacobi"] and res["GS_std"] < res["line_jacobi"]
+
+
+_CLUSTER_CHILD = r"""
+import sys, numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+import lap_gb300 as gb
+from lap_gb300 import gen
+A, b = gen.grid3d_lognormal(40, seed=1002)
+for prec in ("ichol", "GS_std"):
+    s = gb.System.from_csr(A, prec)
+    for p in (1, 2):
+        x, r = s.solve(torch.from_numpy(b).cuda(), tol=1e-9, maxit=5000, precision=p)
+        np.save(f"{sys.argv[2]}_{prec}_{p}.npy", x.cpu().numpy())
+    s.close()
+"""
+
+
+def test_cluster_form_matches_per_cta_form(tmp_path):
+    """The FP32 solves in thread-block clusters pass boundary values through
+    distributed shared memory instead of L2: the arithmetic is the same, so
+    the mixed-precision solutions must be bitwise identical to the per-CTA
+    form's (GBLAP_TRI_CLUSTER=0).  The switch is read once per process."""
+    import os
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = {}
+    for mode in ("0", "8"):
+        env = dict(os.environ, GBLAP_TRI_CLUSTER=mode)
+        stem = str(tmp_path / f"cl{mode}")
+        subprocess.run([sys.executable, "-c", _CLUSTER_CHILD, root, stem], env=env, check=True,
+                       timeout=600)
+        out[mode] = stem
+    for prec in ("ichol", "GS_std"):
+        for p in (1, 2):
+            a = np.load(f"{out['0']}_{prec}_{p}.npy")
+            c = np.load(f"{out['8']}_{prec}_{p}.npy")
+            assert np.array_equal(a, c), (prec, p)
