@@ -4,7 +4,9 @@
 //   * block-diagonal: S Laplacians of uneven size (gb_batch_create), their
 //     CSR concatenated with global row pointers and system-local columns;
 //   * multi-RHS: S right-hand sides on one gb_system (gb_pcg_solve_multi),
-//     the matrix shared and read once per iteration for all columns.
+//     the matrix shared and read once per iteration for all columns; up to
+//     32 right-hand sides run on interleaved vectors ([n][S], transposed on
+//     entry and exit), more on the concatenated layout.
 // Each system runs its own PCG recurrence of cg.c:42-126 -- its own alpha,
 // beta, rho, stopping test and flag -- held in one PcgState per system, so
 // the single-system building blocks (pcg_alpha, pcg_check) apply unchanged.
@@ -418,6 +420,162 @@ __global__ void batch_diag_kernel(BatchArgs B, double* d_r, int* bad) {
   }
 }
 
+// ------------------------------------------------------------ interleaved multi-RHS
+// Multi-RHS with at most 32 right-hand sides keeps its vectors interleaved,
+// v[i * count + s].  A warp takes R = 32 / count rows per step, lane
+// sub * count + s serving row sub of the step and right-hand side s: the
+// warp's vector accesses are one contiguous run, a row's matrix entries are
+// broadcast loads, and a column's values of all right-hand sides are one
+// contiguous load.  Every warp sums its rows in order, folds the R rows of a
+// right-hand side in lane order and writes part[k + 3 * (s * W + warp)]
+// (W = the warps of the grid, the same for every interleaved launch), so the
+// per-system reductions above read system s's partials as the contiguous
+// range [s W, (s + 1) W) -- a fixed order, hence reproducible results.
+enum { IL_RESID = 0, IL_PQ = 1, IL_REPLACE = 2, IL_REPORT = 3 };
+constexpr int kIlBatch = 8;  // entries of a row whose loads are in flight together
+
+struct IlLane {
+  int C, R, sub, s, W, w0;
+  bool ok;  // lanes R * C .. 31 idle
+  __device__ IlLane(const BatchArgs& B) {
+    const int lane = threadIdx.x & 31;
+    C = B.count;
+    R = 32 / C;
+    sub = lane / C;
+    s = lane - sub * C;
+    ok = sub < R;
+    W = gridDim.x * kBatchWarps;
+    w0 = blockIdx.x * kBatchWarps + (threadIdx.x >> 5);
+  }
+  // sum of v over the R lanes of this lane's right-hand side, valid in sub 0
+  __device__ double fold(double v) const {
+    const int lane = threadIdx.x & 31;
+    double t = v;
+    for (int k = 1; k < R; ++k) t += __shfl_sync(0xffffffffu, v, (lane + k * C) & 31);
+    return t;
+  }
+};
+
+template <typename TA, int MODE>
+__global__ void __launch_bounds__(kBatchThreads)
+    bil_row_kernel(BatchArgs B, const TA* __restrict__ a, cudaGraphConditionalHandle cond, int has_cond) {
+  const IlLane L(B);
+  if (MODE == IL_PQ && has_cond && blockIdx.x == 0 && threadIdx.x == 0) {
+    const unsigned g = atomicAdd(&B.tk[2], 1u) + 1u;  // loop guard
+    if (g > (unsigned)B.maxit + 8u) set_cond(cond, true, false);
+  }
+  bool live = false, first = false;
+  double beta = 0.0;
+  if (L.ok) {
+    const PcgState& S = B.st[L.s];
+    if (MODE == IL_RESID || MODE == IL_REPORT) live = true;
+    if (MODE == IL_PQ) {
+      live = !S.done;
+      first = S.iter == 0;
+      beta = first ? 0.0 : S.rho / S.rho_prev;
+    }
+    if (MODE == IL_REPLACE) live = batch_needs_check(B, L.s);
+  }
+  const double* __restrict__ xs = MODE == IL_PQ ? B.w : B.x;  // the operand A multiplies
+  const int C = L.C;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  if (__any_sync(0xffffffffu, live)) {
+    const int ng = (B.n1 + L.R - 1) / L.R;
+    for (int g = L.w0; g < ng; g += L.W) {
+      const int i = g * L.R + L.sub;
+      if (!live || i >= B.n1) continue;
+      const int j0 = __ldg(B.ia + i), j1 = __ldg(B.ia + i + 1);
+      TA acc = TA(0);
+      for (int j = j0; j < j1; j += kIlBatch) {
+        int c[kIlBatch];
+        TA av[kIlBatch], xv[kIlBatch];
+#pragma unroll
+        for (int u = 0; u < kIlBatch; ++u) {
+          c[u] = j + u < j1 ? __ldg(B.ja + j + u) : -1;
+          av[u] = c[u] >= 0 ? __ldg(a + j + u) : TA(0);
+        }
+#pragma unroll
+        for (int u = 0; u < kIlBatch; ++u) xv[u] = c[u] >= 0 ? (TA)__ldg(xs + (size_t)c[u] * C + L.s) : TA(0);
+#pragma unroll
+        for (int u = 0; u < kIlBatch; ++u) acc = fma_rn(av[u], xv[u], acc);
+      }
+      const size_t k = (size_t)i * C + L.s;
+      if (MODE == IL_PQ) {
+        const double wi = B.w[k];
+        const double pi = first ? wi : fma_rn(beta, B.p[k], wi);
+        const double qi = first ? (double)acc : fma_rn(beta, B.q[k], (double)acc);
+        B.p[k] = pi;
+        B.q[k] = qi;
+        a0 = fma_rn(pi, qi, a0);
+      } else {
+        const double bi = B.b[k], ri = bi - (double)acc;
+        a0 += ri * ri;
+        a2 += bi * bi;
+        if (MODE == IL_RESID || MODE == IL_REPLACE) {
+          const double wi = B.jacobi ? B.d_r[i] * ri : ri;
+          B.r[k] = ri;
+          B.w[k] = wi;
+          a1 += ri * wi;
+        }
+      }
+    }
+  }
+  a0 = L.fold(a0);
+  if (MODE != IL_PQ) {
+    a1 = L.fold(a1);
+    a2 = L.fold(a2);
+  }
+  if (L.ok && L.sub == 0 && live) {
+    const size_t slot = 3 * ((size_t)L.s * L.W + L.w0);
+    B.part_b[slot] = a0;
+    if (MODE != IL_PQ) {
+      B.part_b[slot + 1] = a1;
+      B.part_b[slot + 2] = a2;
+    }
+  }
+}
+
+// x += alpha p, r -= alpha q, w = M^-1 r; partials r'r, r'w per (system, warp)
+__global__ void __launch_bounds__(kBatchThreads) bil_update_kernel(BatchArgs B) {
+  const IlLane L(B);
+  const bool live = L.ok && !B.st[L.s].done;
+  const double al = live ? B.st[L.s].spare1 : 0.0;
+  const int C = L.C;
+  double a0 = 0.0, a1 = 0.0;
+  if (__any_sync(0xffffffffu, live)) {
+    const int ng = (B.n1 + L.R - 1) / L.R;
+    for (int g = L.w0; g < ng; g += L.W) {
+      const int i = g * L.R + L.sub;
+      if (!live || i >= B.n1) continue;
+      const size_t k = (size_t)i * C + L.s;
+      B.x[k] = fma_rn(al, B.p[k], B.x[k]);
+      const double ri = fma_rn(-al, B.q[k], B.r[k]);
+      const double wi = B.jacobi ? B.d_r[i] * ri : ri;
+      B.r[k] = ri;
+      B.w[k] = wi;
+      a0 = fma_rn(ri, ri, a0);
+      a1 = fma_rn(ri, wi, a1);
+    }
+  }
+  a0 = L.fold(a0);
+  a1 = L.fold(a1);
+  if (L.ok && L.sub == 0 && live) {
+    B.part_c[2 * ((size_t)L.s * L.W + L.w0)] = a0;
+    B.part_c[2 * ((size_t)L.s * L.W + L.w0) + 1] = a1;
+  }
+}
+
+// [count][n] -> [n][count] (to_il) or back; n * count < 2^31
+__global__ void bil_transpose_kernel(int n, int C, const double* __restrict__ src, double* __restrict__ dst,
+                                     int to_il) {
+  const int N = n * C;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
+    const int i = t / C, s = t - i * C;  // t = i * C + s
+    if (to_il) dst[t] = src[(size_t)s * n + i];
+    else dst[(size_t)s * n + i] = src[t];
+  }
+}
+
 }  // namespace gb
 
 // ================================================================ host side
@@ -426,6 +584,7 @@ using namespace gb;
 struct gb_batch_s {
   int count = 0;
   int shared = 0;  // multi-RHS over one matrix
+  int inter = 0;   // multi-RHS with interleaved vectors (count <= 32)
   int N = 0;       // rows of all systems (the vectors' length)
   int n1 = 0;      // rows of the shared matrix
   int jacobi = 1;
@@ -438,6 +597,7 @@ struct gb_batch_s {
   const double* d_r = nullptr;
   const int* bundles = nullptr;
   int nb = 0, nc = 0;
+  int il_grid = 0;  // interleaved: blocks of every row kernel (nb = its warps)
   std::vector<void*> owned;  // device buffers freed with the batch
   int *row_off = nullptr, *bsys = nullptr, *sys_b = nullptr, *chunk_r0 = nullptr, *csys = nullptr,
       *sys_c = nullptr;
@@ -575,6 +735,16 @@ int grid_chunks(int nc) {
 // One iteration of every live system.
 int batch_body(gb_batch bt, int split, int maxit, cudaGraphConditionalHandle cond, int has_cond) {
   const BatchArgs B = batch_args(bt, maxit);
+  if (bt->inter) {
+    const int G = bt->il_grid;
+    if (split) bil_row_kernel<float, IL_PQ><<<G, kBatchThreads, 0, bt->s>>>(B, bt->a32, cond, has_cond);
+    else bil_row_kernel<double, IL_PQ><<<G, kBatchThreads, 0, bt->s>>>(B, bt->a, cond, has_cond);
+    breduce_alpha_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B);
+    bil_update_kernel<<<G, kBatchThreads, 0, bt->s>>>(B);
+    breduce_check_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B, cond, has_cond);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+  }
   if (split)
     bspmv_pq_kernel<float><<<grid_bundles((const void*)bspmv_pq_kernel<float>, bt->nb, bt->count, bt->shared),
                              kBatchThreads, 0, bt->s>>>(B, bt->a32, cond, has_cond);
@@ -663,11 +833,19 @@ int batch_solve(gb_batch bt, const double* b, double* x, const gb_pcg_opts* opts
   GB_CUDA_TRY(cudaMemcpyAsync(bt->st, hs, sizeof(PcgState) * bt->count, cudaMemcpyHostToDevice, bt->s));
   GB_CUDA_TRY(cudaMemcpyAsync(bt->so, hs + bt->count, sizeof(PcgState) * bt->count, cudaMemcpyHostToDevice, bt->s));
   GB_CUDA_TRY(cudaEventRecord(bt->ev0, bt->s));
-  GB_CUDA_TRY(cudaMemcpyAsync(bt->b, b, bytes, cudaMemcpyDeviceToDevice, bt->s));
-  GB_CUDA_TRY(cudaMemcpyAsync(bt->x, x, bytes, cudaMemcpyDeviceToDevice, bt->s));
+  const int G = bt->il_grid;
+  const int gt = std::max(1, std::min(ceil_div(bt->N, 256), 8 * device_sm_count()));
+  if (bt->inter) {
+    bil_transpose_kernel<<<gt, 256, 0, bt->s>>>(bt->n1, bt->count, b, bt->b, 1);
+    bil_transpose_kernel<<<gt, 256, 0, bt->s>>>(bt->n1, bt->count, x, bt->x, 1);
+  } else {
+    GB_CUDA_TRY(cudaMemcpyAsync(bt->b, b, bytes, cudaMemcpyDeviceToDevice, bt->s));
+    GB_CUDA_TRY(cudaMemcpyAsync(bt->x, x, bytes, cudaMemcpyDeviceToDevice, bt->s));
+  }
   const BatchArgs B = batch_args(bt, o.maxit);
   const int gb64 = grid_bundles((const void*)bresid_kernel, bt->nb, bt->count, bt->shared);
-  bresid_kernel<<<gb64, kBatchThreads, 0, bt->s>>>(B);
+  if (bt->inter) bil_row_kernel<double, IL_RESID><<<G, kBatchThreads, 0, bt->s>>>(B, bt->a, 0, 0);
+  else bresid_kernel<<<gb64, kBatchThreads, 0, bt->s>>>(B);
   breduce_init_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B);
   batch_target_kernel<<<ceil_div(bt->count, 128), 128, 0, bt->s>>>(B);
   GB_CUDA_TRY(cudaGetLastError());
@@ -675,7 +853,8 @@ int batch_solve(gb_batch bt, const double* b, double* x, const gb_pcg_opts* opts
   if (split) {
     for (int round = 0; round < o.max_outer + 1; ++round) {
       GB_CUDA_TRY(cudaMemsetAsync(bt->nactive + 1, 0, sizeof(int), bt->s));
-      btrue_kernel<<<gb64, kBatchThreads, 0, bt->s>>>(B, 1);
+      if (bt->inter) bil_row_kernel<double, IL_REPLACE><<<G, kBatchThreads, 0, bt->s>>>(B, bt->a, 0, 0);
+      else btrue_kernel<<<gb64, kBatchThreads, 0, bt->s>>>(B, 1);
       breduce_outer_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B, 1, itol, o.max_outer);
       GB_CUDA_TRY(cudaGetLastError());
       int resumed = 0;
@@ -685,10 +864,12 @@ int batch_solve(gb_batch bt, const double* b, double* x, const gb_pcg_opts* opts
       GB_TRY(batch_loop(bt, split, o.maxit, o.use_graph));
     }
   }
-  btrue_kernel<<<gb64, kBatchThreads, 0, bt->s>>>(B, 0);
+  if (bt->inter) bil_row_kernel<double, IL_REPORT><<<G, kBatchThreads, 0, bt->s>>>(B, bt->a, 0, 0);
+  else btrue_kernel<<<gb64, kBatchThreads, 0, bt->s>>>(B, 0);
   breduce_outer_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B, 0, itol, o.max_outer);
   GB_CUDA_TRY(cudaGetLastError());
-  GB_CUDA_TRY(cudaMemcpyAsync(x, bt->x, bytes, cudaMemcpyDeviceToDevice, bt->s));
+  if (bt->inter) bil_transpose_kernel<<<gt, 256, 0, bt->s>>>(bt->n1, bt->count, bt->x, x, 0);
+  else GB_CUDA_TRY(cudaMemcpyAsync(x, bt->x, bytes, cudaMemcpyDeviceToDevice, bt->s));
   GB_CUDA_TRY(cudaEventRecord(bt->ev1, bt->s));
   GB_CUDA_TRY(cudaMemcpyAsync(hs, bt->st, sizeof(PcgState) * bt->count, cudaMemcpyDeviceToHost, bt->s));
   GB_CUDA_TRY(cudaMemcpyAsync(hs + bt->count, bt->so, sizeof(PcgState) * bt->count, cudaMemcpyDeviceToHost, bt->s));
@@ -848,11 +1029,27 @@ extern "C" int gb_pcg_solve_multi(gb_system sys, int nrhs, const double* B, doub
     bt->a = sys->a;
     bt->a32 = sys->a32;
     bt->d_r = sys->d_r;
-    bt->bundles = sys->plan.bundles;
-    bt->nb = sys->plan.nbundles;
-    std::vector<int> roff(nrhs + 1);
-    for (int s = 0; s <= nrhs; ++s) roff[s] = s * sys->n;
-    int rc = batch_chunks(bt, roff);
+    int rc = GB_OK;
+    if (nrhs <= 32) {
+      // interleaved vectors; partials per (right-hand side, warp) of a fixed grid
+      bt->inter = 1;
+      const int rows_per_step = 32 / nrhs;
+      const long long steps = (sys->n + rows_per_step - 1) / rows_per_step;
+      const long long cap =
+          (long long)device_sm_count() * occupancy_blocks((const void*)bil_row_kernel<double, IL_PQ>, kBatchThreads);
+      bt->il_grid = (int)std::max(1LL, std::min(cap, (steps + kBatchWarps - 1) / kBatchWarps));
+      bt->nb = bt->il_grid * kBatchWarps;
+      bt->nc = bt->nb * nrhs;
+      std::vector<int> sc(nrhs + 1);
+      for (int s = 0; s <= nrhs; ++s) sc[s] = s * bt->nb;
+      rc = bupload(bt, &bt->sys_c, sc);
+    } else {
+      bt->bundles = sys->plan.bundles;
+      bt->nb = sys->plan.nbundles;
+      std::vector<int> roff(nrhs + 1);
+      for (int s = 0; s <= nrhs; ++s) roff[s] = s * sys->n;
+      rc = batch_chunks(bt, roff);
+    }
     if (rc == GB_OK) rc = batch_buffers(bt);
     if (rc != GB_OK) {
       batch_free(bt);
