@@ -60,6 +60,7 @@ struct BatchArgs {
   const double* d_r;    // [N] (block-diagonal) or [n1] (shared)
   const double* b;
   double *x, *r, *w, *p, *q;
+  float* w32;           // interleaved split precision: w rounded once, the FP32 products' operand
   PcgState* st;         // [count] recurrence
   PcgState* so;         // [count] outer (split precision): target and final state
   double* part_b;       // [3 * nb * (shared ? count : 1)]
@@ -476,7 +477,10 @@ __global__ void __launch_bounds__(kBatchThreads)
     }
     if (MODE == IL_REPLACE) live = batch_needs_check(B, L.s);
   }
-  const double* __restrict__ xs = MODE == IL_PQ ? B.w : B.x;  // the operand A multiplies
+  // the operand A multiplies: w (FP64 or its FP32 copy) or x
+  const TA* __restrict__ xs;
+  if constexpr (sizeof(TA) == 4) xs = B.w32;
+  else xs = MODE == IL_PQ ? B.w : B.x;
   const int C = L.C;
   double a0 = 0.0, a1 = 0.0, a2 = 0.0;
   if (__any_sync(0xffffffffu, live)) {
@@ -495,7 +499,7 @@ __global__ void __launch_bounds__(kBatchThreads)
           av[u] = c[u] >= 0 ? __ldg(a + j + u) : TA(0);
         }
 #pragma unroll
-        for (int u = 0; u < kIlBatch; ++u) xv[u] = c[u] >= 0 ? (TA)__ldg(xs + (size_t)c[u] * C + L.s) : TA(0);
+        for (int u = 0; u < kIlBatch; ++u) xv[u] = c[u] >= 0 ? __ldg(xs + (size_t)c[u] * C + L.s) : TA(0);
 #pragma unroll
         for (int u = 0; u < kIlBatch; ++u) acc = fma_rn(av[u], xv[u], acc);
       }
@@ -515,6 +519,7 @@ __global__ void __launch_bounds__(kBatchThreads)
           const double wi = B.jacobi ? B.d_r[i] * ri : ri;
           B.r[k] = ri;
           B.w[k] = wi;
+          if (B.w32) B.w32[k] = (float)wi;
           a1 += ri * wi;
         }
       }
@@ -553,6 +558,7 @@ __global__ void __launch_bounds__(kBatchThreads) bil_update_kernel(BatchArgs B) 
       const double wi = B.jacobi ? B.d_r[i] * ri : ri;
       B.r[k] = ri;
       B.w[k] = wi;
+      if (B.w32) B.w32[k] = (float)wi;
       a0 = fma_rn(ri, ri, a0);
       a1 = fma_rn(ri, wi, a1);
     }
@@ -602,6 +608,7 @@ struct gb_batch_s {
   int *row_off = nullptr, *bsys = nullptr, *sys_b = nullptr, *chunk_r0 = nullptr, *csys = nullptr,
       *sys_c = nullptr;
   double *b = nullptr, *x = nullptr, *r = nullptr, *w = nullptr, *p = nullptr, *q = nullptr;
+  float* w32 = nullptr;  // interleaved only
   PcgState *st = nullptr, *so = nullptr, *st_h = nullptr;
   double *part_b = nullptr, *part_c = nullptr;
   unsigned* tk = nullptr;
@@ -669,6 +676,7 @@ int batch_chunks(gb_batch bt, const std::vector<int>& row_off) {
 int batch_buffers(gb_batch bt) {
   const size_t N = bt->N;
   for (double** v : {&bt->b, &bt->x, &bt->r, &bt->w, &bt->p, &bt->q}) GB_TRY(balloc(bt, v, N));
+  if (bt->inter) GB_TRY(balloc(bt, &bt->w32, N));
   GB_TRY(balloc(bt, &bt->st, bt->count));
   GB_TRY(balloc(bt, &bt->so, bt->count));
   GB_CUDA_TRY(cudaMallocHost(&bt->st_h, sizeof(PcgState) * 2 * bt->count));
@@ -734,7 +742,8 @@ int grid_chunks(int nc) {
 
 // One iteration of every live system.
 int batch_body(gb_batch bt, int split, int maxit, cudaGraphConditionalHandle cond, int has_cond) {
-  const BatchArgs B = batch_args(bt, maxit);
+  BatchArgs B = batch_args(bt, maxit);
+  if (split) B.w32 = bt->w32;
   if (bt->inter) {
     const int G = bt->il_grid;
     if (split) bil_row_kernel<float, IL_PQ><<<G, kBatchThreads, 0, bt->s>>>(B, bt->a32, cond, has_cond);
@@ -842,7 +851,8 @@ int batch_solve(gb_batch bt, const double* b, double* x, const gb_pcg_opts* opts
     GB_CUDA_TRY(cudaMemcpyAsync(bt->b, b, bytes, cudaMemcpyDeviceToDevice, bt->s));
     GB_CUDA_TRY(cudaMemcpyAsync(bt->x, x, bytes, cudaMemcpyDeviceToDevice, bt->s));
   }
-  const BatchArgs B = batch_args(bt, o.maxit);
+  BatchArgs B = batch_args(bt, o.maxit);
+  if (split) B.w32 = bt->w32;
   const int gb64 = grid_bundles((const void*)bresid_kernel, bt->nb, bt->count, bt->shared);
   if (bt->inter) bil_row_kernel<double, IL_RESID><<<G, kBatchThreads, 0, bt->s>>>(B, bt->a, 0, 0);
   else bresid_kernel<<<gb64, kBatchThreads, 0, bt->s>>>(B);
