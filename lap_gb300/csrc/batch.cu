@@ -46,6 +46,7 @@ constexpr int kChunkRows = 2048;  // rows of one update / reduction chunk
 
 struct BatchArgs {
   int count, N, n1, nb, nc, shared, jacobi;
+  int nbun;             // interleaved: bundles of the shared matrix
   const int* ia;
   const int* ja;
   const int* bundles;   // bundle row starts (global rows, or the shared matrix's rows)
@@ -457,9 +458,29 @@ struct IlLane {
   }
 };
 
+// The row kernels walk the shared matrix's SpMV bundles (<= 32 rows, <=
+// kBundleNnz entries), one warp per bundle: the warp stages the bundle's
+// column indices, values and row starts in shared memory with coalesced
+// loads, then takes the bundle's rows R at a time, kIlRows steps together,
+// so a row's only dependent global loads are its gathers.  A bundle of one
+// row longer than kBundleNnz is read from global memory by lanes of row
+// group 0.
+constexpr int kIlRows = 2;
+
+template <typename TA>
+constexpr size_t il_smem_bytes() {
+  return (size_t)kBatchWarps * (kBundleNnz * (sizeof(int) + sizeof(TA)) + (kBundleRows + 1) * sizeof(int));
+}
+
 template <typename TA, int MODE>
 __global__ void __launch_bounds__(kBatchThreads)
     bil_row_kernel(BatchArgs B, const TA* __restrict__ a, cudaGraphConditionalHandle cond, int has_cond) {
+  extern __shared__ __align__(16) unsigned char il_smem[];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  TA* sa = reinterpret_cast<TA*>(il_smem) + (size_t)wid * kBundleNnz;
+  int* sj = reinterpret_cast<int*>(il_smem + (size_t)kBatchWarps * kBundleNnz * sizeof(TA)) + wid * kBundleNnz;
+  int* sia = reinterpret_cast<int*>(il_smem + (size_t)kBatchWarps * kBundleNnz * (sizeof(TA) + sizeof(int))) +
+             wid * (kBundleRows + 1);
   const IlLane L(B);
   if (MODE == IL_PQ && has_cond && blockIdx.x == 0 && threadIdx.x == 0) {
     const unsigned g = atomicAdd(&B.tk[2], 1u) + 1u;  // loop guard
@@ -484,45 +505,103 @@ __global__ void __launch_bounds__(kBatchThreads)
   const int C = L.C;
   double a0 = 0.0, a1 = 0.0, a2 = 0.0;
   if (__any_sync(0xffffffffu, live)) {
-    const int ng = (B.n1 + L.R - 1) / L.R;
-    for (int g = L.w0; g < ng; g += L.W) {
-      const int i = g * L.R + L.sub;
-      if (!live || i >= B.n1) continue;
-      const int j0 = __ldg(B.ia + i), j1 = __ldg(B.ia + i + 1);
-      TA acc = TA(0);
-      for (int j = j0; j < j1; j += kIlBatch) {
-        int c[kIlBatch];
-        TA av[kIlBatch], xv[kIlBatch];
-#pragma unroll
-        for (int u = 0; u < kIlBatch; ++u) {
-          c[u] = j + u < j1 ? __ldg(B.ja + j + u) : -1;
-          av[u] = c[u] >= 0 ? __ldg(a + j + u) : TA(0);
+    for (int bb = L.w0; bb < B.nbun; bb += L.W) {
+      const int r0 = __ldg(B.bundles + bb), r1 = __ldg(B.bundles + bb + 1);
+      const int j0 = __ldg(B.ia + r0), j1 = __ldg(B.ia + r1);
+      const bool staged = j1 - j0 <= kBundleNnz;  // uniform in the warp
+      if (staged) {
+        for (int e = lane; e < j1 - j0; e += 32) {
+          sj[e] = __ldg(B.ja + j0 + e);
+          sa[e] = __ldg(a + j0 + e);
         }
-#pragma unroll
-        for (int u = 0; u < kIlBatch; ++u) xv[u] = c[u] >= 0 ? __ldg(xs + (size_t)c[u] * C + L.s) : TA(0);
-#pragma unroll
-        for (int u = 0; u < kIlBatch; ++u) acc = fma_rn(av[u], xv[u], acc);
+        if (lane <= r1 - r0) sia[lane] = __ldg(B.ia + r0 + lane) - j0;
+        __syncwarp();
       }
-      const size_t k = (size_t)i * C + L.s;
-      if (MODE == IL_PQ) {
-        const double wi = B.w[k];
-        const double pi = first ? wi : fma_rn(beta, B.p[k], wi);
-        const double qi = first ? (double)acc : fma_rn(beta, B.q[k], (double)acc);
-        B.p[k] = pi;
-        B.q[k] = qi;
-        a0 = fma_rn(pi, qi, a0);
-      } else {
-        const double bi = B.b[k], ri = bi - (double)acc;
-        a0 += ri * ri;
-        a2 += bi * bi;
-        if (MODE == IL_RESID || MODE == IL_REPLACE) {
-          const double wi = B.jacobi ? B.d_r[i] * ri : ri;
-          B.r[k] = ri;
-          B.w[k] = wi;
-          if (B.w32) B.w32[k] = (float)wi;
-          a1 += ri * wi;
+      const int steps = (r1 - r0 + L.R - 1) / L.R;
+      for (int t = 0; t < steps; t += kIlRows) {
+        int i[kIlRows], e0[kIlRows], e1[kIlRows];
+        bool v[kIlRows];
+        double o0[kIlRows], o1[kIlRows], o2[kIlRows];  // own-row operands, loaded up front
+#pragma unroll
+        for (int r = 0; r < kIlRows; ++r) {
+          i[r] = r0 + (t + r) * L.R + L.sub;
+          v[r] = live && i[r] < r1;
+          const size_t k = (size_t)(v[r] ? i[r] : 0) * C + L.s;
+          if (MODE == IL_PQ) {
+            o0[r] = v[r] ? B.w[k] : 0.0;
+            o1[r] = v[r] && !first ? B.p[k] : 0.0;
+            o2[r] = v[r] && !first ? B.q[k] : 0.0;
+          } else {
+            o0[r] = v[r] ? B.b[k] : 0.0;
+            o1[r] = v[r] && B.jacobi && MODE != IL_REPORT ? B.d_r[i[r]] : 0.0;
+            o2[r] = 0.0;
+          }
+          e0[r] = !v[r] ? 0 : staged ? sia[i[r] - r0] : __ldg(B.ia + i[r]) - j0;
+          e1[r] = !v[r] ? 0 : staged ? sia[i[r] - r0 + 1] : __ldg(B.ia + i[r] + 1) - j0;
+        }
+        // first kIlBatch entries of every row: all gathers issued before any use
+        TA xv[kIlRows][kIlBatch], acc[kIlRows];
+        int cc[kIlRows][kIlBatch];
+#pragma unroll
+        for (int r = 0; r < kIlRows; ++r)
+#pragma unroll
+          for (int u = 0; u < kIlBatch; ++u) {
+            const int e = e0[r] + u;
+            cc[r][u] = e < e1[r] ? (staged ? sj[e] : __ldg(B.ja + j0 + e)) : -1;
+          }
+#pragma unroll
+        for (int r = 0; r < kIlRows; ++r)
+#pragma unroll
+          for (int u = 0; u < kIlBatch; ++u) xv[r][u] = cc[r][u] >= 0 ? __ldg(xs + (size_t)cc[r][u] * C + L.s) : TA(0);
+#pragma unroll
+        for (int r = 0; r < kIlRows; ++r) {
+          acc[r] = TA(0);
+#pragma unroll
+          for (int u = 0; u < kIlBatch; ++u) {
+            const int e = e0[r] + u;
+            if (e < e1[r]) acc[r] = fma_rn(staged ? sa[e] : __ldg(a + j0 + e), xv[r][u], acc[r]);
+          }
+        }
+        // the rest of longer rows, row by row
+#pragma unroll
+        for (int r = 0; r < kIlRows; ++r)
+          for (int e = e0[r] + kIlBatch; e < e1[r]; e += kIlBatch) {
+            TA xx[kIlBatch];
+#pragma unroll
+            for (int u = 0; u < kIlBatch; ++u) {
+              const int c = e + u < e1[r] ? (staged ? sj[e + u] : __ldg(B.ja + j0 + e + u)) : -1;
+              xx[u] = c >= 0 ? __ldg(xs + (size_t)c * C + L.s) : TA(0);
+            }
+#pragma unroll
+            for (int u = 0; u < kIlBatch; ++u)
+              if (e + u < e1[r]) acc[r] = fma_rn(staged ? sa[e + u] : __ldg(a + j0 + e + u), xx[u], acc[r]);
+          }
+#pragma unroll
+        for (int r = 0; r < kIlRows; ++r) {
+          if (!v[r]) continue;
+          const size_t k = (size_t)i[r] * C + L.s;
+          if (MODE == IL_PQ) {
+            const double wi = o0[r];
+            const double pi = first ? wi : fma_rn(beta, o1[r], wi);
+            const double qi = first ? (double)acc[r] : fma_rn(beta, o2[r], (double)acc[r]);
+            B.p[k] = pi;
+            B.q[k] = qi;
+            a0 = fma_rn(pi, qi, a0);
+          } else {
+            const double bi = o0[r], ri = bi - (double)acc[r];
+            a0 += ri * ri;
+            a2 += bi * bi;
+            if (MODE == IL_RESID || MODE == IL_REPLACE) {
+              const double wi = B.jacobi ? o1[r] * ri : ri;
+              B.r[k] = ri;
+              B.w[k] = wi;
+              if (B.w32) B.w32[k] = (float)wi;
+              a1 += ri * wi;
+            }
+          }
         }
       }
+      __syncwarp();  // the staging buffers are refilled by the next bundle
     }
   }
   a0 = L.fold(a0);
@@ -571,14 +650,36 @@ __global__ void __launch_bounds__(kBatchThreads) bil_update_kernel(BatchArgs B) 
   }
 }
 
-// [count][n] -> [n][count] (to_il) or back; n * count < 2^31
-__global__ void bil_transpose_kernel(int n, int C, const double* __restrict__ src, double* __restrict__ dst,
-                                     int to_il) {
-  const int N = n * C;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
-    const int i = t / C, s = t - i * C;  // t = i * C + s
-    if (to_il) dst[t] = src[(size_t)s * n + i];
-    else dst[(size_t)s * n + i] = src[t];
+// [count][n] -> [n][count] (to_il) or back, 64 rows per tile through shared
+// memory, so both the strided and the interleaved side are coalesced.
+constexpr int kTrRows = 64;
+__global__ void __launch_bounds__(256) bil_transpose_kernel(int n, int C, const double* __restrict__ src,
+                                                            double* __restrict__ dst, int to_il) {
+  __shared__ double t[32][kTrRows + 1];  // [s][row - i0]
+  for (int i0 = blockIdx.x * kTrRows; i0 < n; i0 += gridDim.x * kTrRows) {
+    const int rows = min(kTrRows, n - i0);
+    if (to_il) {
+      for (int e = threadIdx.x; e < C * kTrRows; e += blockDim.x) {
+        const int sr = e / kTrRows, r = e - sr * kTrRows;
+        if (r < rows) t[sr][r] = src[(size_t)sr * n + i0 + r];
+      }
+      __syncthreads();
+      for (int e = threadIdx.x; e < rows * C; e += blockDim.x) {
+        const int r = e / C, sr = e - r * C;
+        dst[(size_t)i0 * C + e] = t[sr][r];
+      }
+    } else {
+      for (int e = threadIdx.x; e < rows * C; e += blockDim.x) {
+        const int r = e / C, sr = e - r * C;
+        t[sr][r] = src[(size_t)i0 * C + e];
+      }
+      __syncthreads();
+      for (int e = threadIdx.x; e < C * kTrRows; e += blockDim.x) {
+        const int sr = e / kTrRows, r = e - sr * kTrRows;
+        if (r < rows) dst[(size_t)sr * n + i0 + r] = t[sr][r];
+      }
+    }
+    __syncthreads();  // the tile is refilled by the next step
   }
 }
 
@@ -604,6 +705,7 @@ struct gb_batch_s {
   const int* bundles = nullptr;
   int nb = 0, nc = 0;
   int il_grid = 0;  // interleaved: blocks of every row kernel (nb = its warps)
+  int nbun = 0;     // interleaved: bundles of the shared matrix
   std::vector<void*> owned;  // device buffers freed with the batch
   int *row_off = nullptr, *bsys = nullptr, *sys_b = nullptr, *chunk_r0 = nullptr, *csys = nullptr,
       *sys_c = nullptr;
@@ -698,6 +800,7 @@ BatchArgs batch_args(gb_batch bt, int maxit) {
   B.N = bt->N;
   B.n1 = bt->n1;
   B.nb = bt->nb;
+  B.nbun = bt->nbun;
   B.nc = bt->nc;
   B.shared = bt->shared;
   B.jacobi = bt->jacobi;
@@ -740,14 +843,34 @@ int grid_chunks(int nc) {
   return std::max(1, std::min(nc, device_sm_count() * occupancy_blocks((const void*)bupdate_kernel, kBatchThreads)));
 }
 
+// Interleaved row kernels: dynamic shared memory for the bundle staging.
+template <typename TA, int MODE>
+void il_rows(gb_batch bt, const BatchArgs& B, const TA* a, cudaGraphConditionalHandle cond, int has_cond) {
+  bil_row_kernel<TA, MODE><<<bt->il_grid, kBatchThreads, il_smem_bytes<TA>(), bt->s>>>(B, a, cond, has_cond);
+}
+template <typename TA, int MODE>
+int il_attr() {
+  GB_CUDA_TRY(cudaFuncSetAttribute((const void*)bil_row_kernel<TA, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)il_smem_bytes<TA>()));
+  return GB_OK;
+}
+int il_setup() {
+  GB_TRY((il_attr<double, IL_RESID>()));
+  GB_TRY((il_attr<double, IL_PQ>()));
+  GB_TRY((il_attr<float, IL_PQ>()));
+  GB_TRY((il_attr<double, IL_REPLACE>()));
+  GB_TRY((il_attr<double, IL_REPORT>()));
+  return GB_OK;
+}
+
 // One iteration of every live system.
 int batch_body(gb_batch bt, int split, int maxit, cudaGraphConditionalHandle cond, int has_cond) {
   BatchArgs B = batch_args(bt, maxit);
   if (split) B.w32 = bt->w32;
   if (bt->inter) {
     const int G = bt->il_grid;
-    if (split) bil_row_kernel<float, IL_PQ><<<G, kBatchThreads, 0, bt->s>>>(B, bt->a32, cond, has_cond);
-    else bil_row_kernel<double, IL_PQ><<<G, kBatchThreads, 0, bt->s>>>(B, bt->a, cond, has_cond);
+    if (split) il_rows<float, IL_PQ>(bt, B, bt->a32, cond, has_cond);
+    else il_rows<double, IL_PQ>(bt, B, bt->a, cond, has_cond);
     breduce_alpha_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B);
     bil_update_kernel<<<G, kBatchThreads, 0, bt->s>>>(B);
     breduce_check_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B, cond, has_cond);
@@ -842,8 +965,7 @@ int batch_solve(gb_batch bt, const double* b, double* x, const gb_pcg_opts* opts
   GB_CUDA_TRY(cudaMemcpyAsync(bt->st, hs, sizeof(PcgState) * bt->count, cudaMemcpyHostToDevice, bt->s));
   GB_CUDA_TRY(cudaMemcpyAsync(bt->so, hs + bt->count, sizeof(PcgState) * bt->count, cudaMemcpyHostToDevice, bt->s));
   GB_CUDA_TRY(cudaEventRecord(bt->ev0, bt->s));
-  const int G = bt->il_grid;
-  const int gt = std::max(1, std::min(ceil_div(bt->N, 256), 8 * device_sm_count()));
+  const int gt = std::max(1, std::min(ceil_div(bt->n1, kTrRows), 8 * device_sm_count()));
   if (bt->inter) {
     bil_transpose_kernel<<<gt, 256, 0, bt->s>>>(bt->n1, bt->count, b, bt->b, 1);
     bil_transpose_kernel<<<gt, 256, 0, bt->s>>>(bt->n1, bt->count, x, bt->x, 1);
@@ -854,7 +976,7 @@ int batch_solve(gb_batch bt, const double* b, double* x, const gb_pcg_opts* opts
   BatchArgs B = batch_args(bt, o.maxit);
   if (split) B.w32 = bt->w32;
   const int gb64 = grid_bundles((const void*)bresid_kernel, bt->nb, bt->count, bt->shared);
-  if (bt->inter) bil_row_kernel<double, IL_RESID><<<G, kBatchThreads, 0, bt->s>>>(B, bt->a, 0, 0);
+  if (bt->inter) il_rows<double, IL_RESID>(bt, B, bt->a, 0, 0);
   else bresid_kernel<<<gb64, kBatchThreads, 0, bt->s>>>(B);
   breduce_init_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B);
   batch_target_kernel<<<ceil_div(bt->count, 128), 128, 0, bt->s>>>(B);
@@ -863,7 +985,7 @@ int batch_solve(gb_batch bt, const double* b, double* x, const gb_pcg_opts* opts
   if (split) {
     for (int round = 0; round < o.max_outer + 1; ++round) {
       GB_CUDA_TRY(cudaMemsetAsync(bt->nactive + 1, 0, sizeof(int), bt->s));
-      if (bt->inter) bil_row_kernel<double, IL_REPLACE><<<G, kBatchThreads, 0, bt->s>>>(B, bt->a, 0, 0);
+      if (bt->inter) il_rows<double, IL_REPLACE>(bt, B, bt->a, 0, 0);
       else btrue_kernel<<<gb64, kBatchThreads, 0, bt->s>>>(B, 1);
       breduce_outer_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B, 1, itol, o.max_outer);
       GB_CUDA_TRY(cudaGetLastError());
@@ -874,7 +996,7 @@ int batch_solve(gb_batch bt, const double* b, double* x, const gb_pcg_opts* opts
       GB_TRY(batch_loop(bt, split, o.maxit, o.use_graph));
     }
   }
-  if (bt->inter) bil_row_kernel<double, IL_REPORT><<<G, kBatchThreads, 0, bt->s>>>(B, bt->a, 0, 0);
+  if (bt->inter) il_rows<double, IL_REPORT>(bt, B, bt->a, 0, 0);
   else btrue_kernel<<<gb64, kBatchThreads, 0, bt->s>>>(B, 0);
   breduce_outer_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B, 0, itol, o.max_outer);
   GB_CUDA_TRY(cudaGetLastError());
@@ -1043,16 +1165,18 @@ extern "C" int gb_pcg_solve_multi(gb_system sys, int nrhs, const double* B, doub
     if (nrhs <= 32) {
       // interleaved vectors; partials per (right-hand side, warp) of a fixed grid
       bt->inter = 1;
-      const int rows_per_step = 32 / nrhs;
-      const long long steps = (sys->n + rows_per_step - 1) / rows_per_step;
-      const long long cap =
-          (long long)device_sm_count() * occupancy_blocks((const void*)bil_row_kernel<double, IL_PQ>, kBatchThreads);
-      bt->il_grid = (int)std::max(1LL, std::min(cap, (steps + kBatchWarps - 1) / kBatchWarps));
+      bt->bundles = sys->plan.bundles;
+      bt->nbun = sys->plan.nbundles;
+      rc = il_setup();
+      const long long cap = (long long)device_sm_count() *
+                            occupancy_blocks((const void*)bil_row_kernel<double, IL_PQ>, kBatchThreads,
+                                             il_smem_bytes<double>());
+      bt->il_grid = (int)std::max(1LL, std::min(cap, ((long long)bt->nbun + kBatchWarps - 1) / kBatchWarps));
       bt->nb = bt->il_grid * kBatchWarps;
       bt->nc = bt->nb * nrhs;
       std::vector<int> sc(nrhs + 1);
       for (int s = 0; s <= nrhs; ++s) sc[s] = s * bt->nb;
-      rc = bupload(bt, &bt->sys_c, sc);
+      if (rc == GB_OK) rc = bupload(bt, &bt->sys_c, sc);
     } else {
       bt->bundles = sys->plan.bundles;
       bt->nb = sys->plan.nbundles;
