@@ -514,7 +514,8 @@ __global__ void __launch_bounds__(kBatchThreads)
           sj[e] = __ldg(B.ja + j0 + e);
           sa[e] = __ldg(a + j0 + e);
         }
-        if (lane <= r1 - r0) sia[lane] = __ldg(B.ia + r0 + lane) - j0;
+        if (lane < r1 - r0) sia[lane] = __ldg(B.ia + r0 + lane) - j0;
+        if (lane == 0) sia[r1 - r0] = j1 - j0;  // end of the last row (r1 - r0 <= 32)
         __syncwarp();
       }
       const int steps = (r1 - r0 + L.R - 1) / L.R;
@@ -1146,7 +1147,10 @@ extern "C" int gb_pcg_solve_multi(gb_system sys, int nrhs, const double* B, doub
   if (sys->prec != GB_PREC_LINE_JACOBI && sys->prec != GB_PREC_NONE) return GB_NOT_SUPPORTED;
   if ((long long)nrhs * sys->n >= (1LL << 31) - 1) return GB_NOT_SUPPORTED;
   gb_batch bt = sys->multi;
-  if (!bt || bt->count != nrhs) {
+  // rebuilt when the count changes or the system's SpMV plan was rebuilt (autotuning)
+  const bool stale = bt && (bt->bundles != sys->plan.bundles ||
+                            (bt->inter ? bt->nbun : bt->nb) != sys->plan.nbundles);
+  if (!bt || bt->count != nrhs || stale) {
     if (bt) batch_free(bt);
     sys->multi = nullptr;
     bt = new gb_batch_s();
