@@ -69,6 +69,11 @@ struct BatchArgs {
   unsigned* tk;         // [0] check ticket, [1] outer ticket, [2] loop guard
   int* nactive;         // [0] running systems, [1] systems to resume
   int maxit;
+  // interleaved split precision: residual replacement inside the loop
+  int il_inline;
+  int* rep;             // [count] 1 while a system's replacement is being applied
+  double delta;         // inner tolerance of a resumed recurrence (relative)
+  int max_outer;
 };
 
 // x operand of the system whose vectors start at `off`, rounded to the
@@ -343,6 +348,39 @@ __global__ void __launch_bounds__(kBatchThreads) btrue_kernel(BatchArgs B, int r
   });
 }
 
+// The refinement decision of a system whose FP64 residual was recomputed
+// (||r||^2 = v0, r'w = v1): final when it meets the target (or replacements
+// ran out), otherwise the recurrence resumes with the threshold
+// max(delta*||r||, target) and rho of the replaced residual (returns true).
+__device__ __forceinline__ bool outer_decide(const BatchArgs& B, PcgState& S, PcgState& O, double v0, double v1,
+                                             double delta, int max_outer) {
+  const double rt = sqrt(v0);
+  O.rr = v0;
+  O.iter += 1;  // replacements
+  if (!(rt == rt) || isinf(rt)) {
+    O.done = 1;
+    O.flag = 2;
+    O.status = GB_BREAKDOWN;
+  } else if (rt < O.tolrel) {
+    O.done = 1;
+    O.flag = 0;
+    O.status = GB_OK;
+  } else if (O.iter >= max_outer || S.iter > S.maxit) {
+    O.done = 1;
+    O.flag = 1;
+    O.status = GB_MAXIT;
+  } else {
+    S.done = 0;
+    S.flag = 1;
+    S.status = GB_OK;
+    S.tolrel = fmax(delta * rt, O.tolrel);
+    S.rho_prev = S.rho;
+    S.rho = B.jacobi ? v1 : v0;
+    return true;
+  }
+  return false;
+}
+
 // replace = 1: the refinement decision per checked system -- final when the
 // FP64 residual meets the target (or replacements ran out), otherwise the
 // recurrence resumes with the threshold max(delta*||r||, target) and rho of
@@ -373,29 +411,7 @@ __global__ void __launch_bounds__(kBatchThreads)
     O.rho = sqrt(v2);
     return;
   }
-  O.rr = v0;
-  O.iter += 1;  // replacements
-  if (!(rt == rt) || isinf(rt)) {
-    O.done = 1;
-    O.flag = 2;
-    O.status = GB_BREAKDOWN;
-  } else if (rt < O.tolrel) {
-    O.done = 1;
-    O.flag = 0;
-    O.status = GB_OK;
-  } else if (O.iter >= max_outer || S.iter > S.maxit) {
-    O.done = 1;
-    O.flag = 1;
-    O.status = GB_MAXIT;
-  } else {
-    S.done = 0;
-    S.flag = 1;
-    S.status = GB_OK;
-    S.tolrel = fmax(delta * rt, O.tolrel);
-    S.rho_prev = S.rho;
-    S.rho = B.jacobi ? v1 : v0;
-    atomicAdd(&B.nactive[1], 1);
-  }
+  if (outer_decide(B, S, O, v0, v1, delta, max_outer)) atomicAdd(&B.nactive[1], 1);
 }
 
 // target of the refinement: tol * ||b - A x0|| (the recurrence's res0)
@@ -461,12 +477,15 @@ struct IlLane {
 // The row kernels walk the shared matrix's SpMV bundles (<= 32 rows, <=
 // kBundleNnz entries), one warp per bundle: the warp stages the bundle's
 // column indices, values and row starts in shared memory with coalesced
-// loads, then takes the bundle's rows R at a time, kIlRows steps together,
-// so a row's only dependent global loads are its gathers.  A bundle of one
-// row longer than kBundleNnz is read from global memory by lanes of row
-// group 0.
-constexpr int kIlRows = 2;
-
+// loads, then takes the bundle's rows R at a time, so a row's only dependent
+// global loads are its gathers (kIlBatch of them in flight).  A bundle of
+// one row longer than kBundleNnz is read from global memory by row group 0.
+//
+// Split precision (il_inline): a system whose recurrence paused at its
+// inner threshold gets its FP64 residual in the next iteration's A w pass:
+// its lanes compute r = b - A x with the FP64 values and x while the other
+// lanes compute their FP32 products, so no system waits for the others to
+// pause.  Warps without such a lane take the FP32-only path.
 template <typename TA>
 constexpr size_t il_smem_bytes() {
   return (size_t)kBatchWarps * (kBundleNnz * (sizeof(int) + sizeof(TA)) + (kBundleRows + 1) * sizeof(int));
@@ -486,7 +505,8 @@ __global__ void __launch_bounds__(kBatchThreads)
     const unsigned g = atomicAdd(&B.tk[2], 1u) + 1u;  // loop guard
     if (g > (unsigned)B.maxit + 8u) set_cond(cond, true, false);
   }
-  bool live = false, first = false;
+  constexpr bool kInline = MODE == IL_PQ && sizeof(TA) == 4;
+  bool live = false, rep = false, first = false;
   double beta = 0.0;
   if (L.ok) {
     const PcgState& S = B.st[L.s];
@@ -495,6 +515,7 @@ __global__ void __launch_bounds__(kBatchThreads)
       live = !S.done;
       first = S.iter == 0;
       beta = first ? 0.0 : S.rho / S.rho_prev;
+      if (kInline && B.il_inline) rep = batch_needs_check(B, L.s);
     }
     if (MODE == IL_REPLACE) live = batch_needs_check(B, L.s);
   }
@@ -503,8 +524,9 @@ __global__ void __launch_bounds__(kBatchThreads)
   if constexpr (sizeof(TA) == 4) xs = B.w32;
   else xs = MODE == IL_PQ ? B.w : B.x;
   const int C = L.C;
+  const bool anyrep = kInline && __any_sync(0xffffffffu, rep);  // uniform in the warp
   double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-  if (__any_sync(0xffffffffu, live)) {
+  if (__any_sync(0xffffffffu, live || rep)) {
     for (int bb = L.w0; bb < B.nbun; bb += L.W) {
       const int r0 = __ldg(B.bundles + bb), r1 = __ldg(B.bundles + bb + 1);
       const int j0 = __ldg(B.ia + r0), j1 = __ldg(B.ia + r1);
@@ -518,87 +540,62 @@ __global__ void __launch_bounds__(kBatchThreads)
         if (lane == 0) sia[r1 - r0] = j1 - j0;  // end of the last row (r1 - r0 <= 32)
         __syncwarp();
       }
-      const int steps = (r1 - r0 + L.R - 1) / L.R;
-      for (int t = 0; t < steps; t += kIlRows) {
-        int i[kIlRows], e0[kIlRows], e1[kIlRows];
-        bool v[kIlRows];
-        double o0[kIlRows], o1[kIlRows], o2[kIlRows];  // own-row operands, loaded up front
-#pragma unroll
-        for (int r = 0; r < kIlRows; ++r) {
-          i[r] = r0 + (t + r) * L.R + L.sub;
-          v[r] = live && i[r] < r1;
-          const size_t k = (size_t)(v[r] ? i[r] : 0) * C + L.s;
-          if (MODE == IL_PQ) {
-            o0[r] = v[r] ? B.w[k] : 0.0;
-            o1[r] = v[r] && !first ? B.p[k] : 0.0;
-            o2[r] = v[r] && !first ? B.q[k] : 0.0;
-          } else {
-            o0[r] = v[r] ? B.b[k] : 0.0;
-            o1[r] = v[r] && B.jacobi && MODE != IL_REPORT ? B.d_r[i[r]] : 0.0;
-            o2[r] = 0.0;
-          }
-          e0[r] = !v[r] ? 0 : staged ? sia[i[r] - r0] : __ldg(B.ia + i[r]) - j0;
-          e1[r] = !v[r] ? 0 : staged ? sia[i[r] - r0 + 1] : __ldg(B.ia + i[r] + 1) - j0;
+      for (int i = r0 + L.sub; i - L.sub < r1; i += L.R) {
+        const bool v = (live || rep) && i < r1;
+        const size_t k = (size_t)(v ? i : 0) * C + L.s;
+        // own-row operands, loaded before the gathers
+        double o0, o1 = 0.0, o2 = 0.0;
+        if (MODE == IL_PQ && !rep) {
+          o0 = v ? B.w[k] : 0.0;
+          o1 = v && !first ? B.p[k] : 0.0;
+          o2 = v && !first ? B.q[k] : 0.0;
+        } else {
+          o0 = v ? B.b[k] : 0.0;
+          o1 = v && B.jacobi && MODE != IL_REPORT ? B.d_r[i] : 0.0;
         }
-        // first kIlBatch entries of every row: all gathers issued before any use
-        TA xv[kIlRows][kIlBatch], acc[kIlRows];
-        int cc[kIlRows][kIlBatch];
+        const int e0 = !v ? 0 : staged ? sia[i - r0] : __ldg(B.ia + i) - j0;
+        const int e1 = !v ? 0 : staged ? sia[i - r0 + 1] : __ldg(B.ia + i + 1) - j0;
+        TA acc = TA(0);
+        double acc64 = 0.0;  // inline replacement: FP64 A x
+        for (int e = e0; e < e1; e += kIlBatch) {
+          int cc[kIlBatch];
+          TA xv[kIlBatch];
 #pragma unroll
-        for (int r = 0; r < kIlRows; ++r)
+          for (int u = 0; u < kIlBatch; ++u)
+            cc[u] = e + u < e1 ? (staged ? sj[e + u] : __ldg(B.ja + j0 + e + u)) : -1;
+          if (!kInline || !rep) {
 #pragma unroll
-          for (int u = 0; u < kIlBatch; ++u) {
-            const int e = e0[r] + u;
-            cc[r][u] = e < e1[r] ? (staged ? sj[e] : __ldg(B.ja + j0 + e)) : -1;
-          }
-#pragma unroll
-        for (int r = 0; r < kIlRows; ++r)
-#pragma unroll
-          for (int u = 0; u < kIlBatch; ++u) xv[r][u] = cc[r][u] >= 0 ? __ldg(xs + (size_t)cc[r][u] * C + L.s) : TA(0);
-#pragma unroll
-        for (int r = 0; r < kIlRows; ++r) {
-          acc[r] = TA(0);
-#pragma unroll
-          for (int u = 0; u < kIlBatch; ++u) {
-            const int e = e0[r] + u;
-            if (e < e1[r]) acc[r] = fma_rn(staged ? sa[e] : __ldg(a + j0 + e), xv[r][u], acc[r]);
-          }
-        }
-        // the rest of longer rows, row by row
-#pragma unroll
-        for (int r = 0; r < kIlRows; ++r)
-          for (int e = e0[r] + kIlBatch; e < e1[r]; e += kIlBatch) {
-            TA xx[kIlBatch];
-#pragma unroll
-            for (int u = 0; u < kIlBatch; ++u) {
-              const int c = e + u < e1[r] ? (staged ? sj[e + u] : __ldg(B.ja + j0 + e + u)) : -1;
-              xx[u] = c >= 0 ? __ldg(xs + (size_t)c * C + L.s) : TA(0);
-            }
+            for (int u = 0; u < kIlBatch; ++u) xv[u] = cc[u] >= 0 ? __ldg(xs + (size_t)cc[u] * C + L.s) : TA(0);
 #pragma unroll
             for (int u = 0; u < kIlBatch; ++u)
-              if (e + u < e1[r]) acc[r] = fma_rn(staged ? sa[e + u] : __ldg(a + j0 + e + u), xx[u], acc[r]);
-          }
-#pragma unroll
-        for (int r = 0; r < kIlRows; ++r) {
-          if (!v[r]) continue;
-          const size_t k = (size_t)i[r] * C + L.s;
-          if (MODE == IL_PQ) {
-            const double wi = o0[r];
-            const double pi = first ? wi : fma_rn(beta, o1[r], wi);
-            const double qi = first ? (double)acc[r] : fma_rn(beta, o2[r], (double)acc[r]);
-            B.p[k] = pi;
-            B.q[k] = qi;
-            a0 = fma_rn(pi, qi, a0);
+              if (cc[u] >= 0) acc = fma_rn(staged ? sa[e + u] : __ldg(a + j0 + e + u), xv[u], acc);
           } else {
-            const double bi = o0[r], ri = bi - (double)acc[r];
-            a0 += ri * ri;
-            a2 += bi * bi;
-            if (MODE == IL_RESID || MODE == IL_REPLACE) {
-              const double wi = B.jacobi ? o1[r] * ri : ri;
-              B.r[k] = ri;
-              B.w[k] = wi;
-              if (B.w32) B.w32[k] = (float)wi;
-              a1 += ri * wi;
-            }
+            double xd[kIlBatch];
+#pragma unroll
+            for (int u = 0; u < kIlBatch; ++u) xd[u] = cc[u] >= 0 ? __ldg(B.x + (size_t)cc[u] * C + L.s) : 0.0;
+#pragma unroll
+            for (int u = 0; u < kIlBatch; ++u)
+              if (cc[u] >= 0) acc64 = fma_rn(__ldg(B.a + j0 + e + u), xd[u], acc64);
+          }
+        }
+        if (!v) continue;
+        if (MODE == IL_PQ && !rep) {
+          const double wi = o0;
+          const double pi = first ? wi : fma_rn(beta, o1, wi);
+          const double qi = first ? (double)acc : fma_rn(beta, o2, (double)acc);
+          B.p[k] = pi;
+          B.q[k] = qi;
+          a0 = fma_rn(pi, qi, a0);
+        } else {
+          const double bi = o0, ri = bi - (rep ? acc64 : (double)acc);
+          a0 += ri * ri;
+          a2 += bi * bi;
+          if (MODE != IL_REPORT) {
+            const double wi = B.jacobi ? o1 * ri : ri;
+            B.r[k] = ri;
+            B.w[k] = wi;
+            if (B.w32) B.w32[k] = (float)wi;
+            a1 += ri * wi;
           }
         }
       }
@@ -606,41 +603,65 @@ __global__ void __launch_bounds__(kBatchThreads)
     }
   }
   a0 = L.fold(a0);
-  if (MODE != IL_PQ) {
+  if (MODE != IL_PQ || anyrep) {
     a1 = L.fold(a1);
     a2 = L.fold(a2);
   }
-  if (L.ok && L.sub == 0 && live) {
+  if (L.ok && L.sub == 0 && (live || rep)) {
     const size_t slot = 3 * ((size_t)L.s * L.W + L.w0);
     B.part_b[slot] = a0;
-    if (MODE != IL_PQ) {
+    if (MODE != IL_PQ || rep) {
       B.part_b[slot + 1] = a1;
       B.part_b[slot + 2] = a2;
     }
   }
 }
 
-// x += alpha p, r -= alpha q, w = M^-1 r; partials r'r, r'w per (system, warp)
+// x += alpha p, r -= alpha q, w = M^-1 r; partials r'r, r'w per (system,
+// warp) at part_c[2 * (s * Wu + warp)], Wu = this grid's warps (its own,
+// larger than the row kernels').  Each lane takes kIlUpd row steps per pass,
+// all their loads issued before any store.
+constexpr int kIlUpd = 2;
+
 __global__ void __launch_bounds__(kBatchThreads) bil_update_kernel(BatchArgs B) {
   const IlLane L(B);
-  const bool live = L.ok && !B.st[L.s].done;
+  const bool live = L.ok && !B.st[L.s].done && !(B.il_inline && B.rep[L.s]);
   const double al = live ? B.st[L.s].spare1 : 0.0;
   const int C = L.C;
+  const double* __restrict__ xv = B.x;
+  const double* __restrict__ pv = B.p;
+  const double* __restrict__ qv = B.q;
+  const double* __restrict__ rv = B.r;
   double a0 = 0.0, a1 = 0.0;
   if (__any_sync(0xffffffffu, live)) {
     const int ng = (B.n1 + L.R - 1) / L.R;
-    for (int g = L.w0; g < ng; g += L.W) {
-      const int i = g * L.R + L.sub;
-      if (!live || i >= B.n1) continue;
-      const size_t k = (size_t)i * C + L.s;
-      B.x[k] = fma_rn(al, B.p[k], B.x[k]);
-      const double ri = fma_rn(-al, B.q[k], B.r[k]);
-      const double wi = B.jacobi ? B.d_r[i] * ri : ri;
-      B.r[k] = ri;
-      B.w[k] = wi;
-      if (B.w32) B.w32[k] = (float)wi;
-      a0 = fma_rn(ri, ri, a0);
-      a1 = fma_rn(ri, wi, a1);
+    for (int g = L.w0; g < ng; g += kIlUpd * L.W) {
+      double x[kIlUpd], p[kIlUpd], q[kIlUpd], r[kIlUpd], d[kIlUpd];
+      bool v[kIlUpd];
+      size_t k[kIlUpd];
+#pragma unroll
+      for (int u = 0; u < kIlUpd; ++u) {
+        const int i = (g + u * L.W) * L.R + L.sub;
+        v[u] = live && g + u * L.W < ng && i < B.n1;
+        k[u] = (size_t)(v[u] ? i : 0) * C + L.s;
+        x[u] = v[u] ? xv[k[u]] : 0.0;
+        p[u] = v[u] ? pv[k[u]] : 0.0;
+        q[u] = v[u] ? qv[k[u]] : 0.0;
+        r[u] = v[u] ? rv[k[u]] : 0.0;
+        d[u] = v[u] && B.jacobi ? B.d_r[i] : 1.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kIlUpd; ++u) {
+        if (!v[u]) continue;
+        const double ri = fma_rn(-al, q[u], r[u]);
+        const double wi = B.jacobi ? d[u] * ri : ri;
+        B.x[k[u]] = fma_rn(al, p[u], x[u]);
+        B.r[k[u]] = ri;
+        B.w[k[u]] = wi;
+        if (B.w32) B.w32[k[u]] = (float)wi;
+        a0 = fma_rn(ri, ri, a0);
+        a1 = fma_rn(ri, wi, a1);
+      }
     }
   }
   a0 = L.fold(a0);
@@ -649,6 +670,76 @@ __global__ void __launch_bounds__(kBatchThreads) bil_update_kernel(BatchArgs B) 
     B.part_c[2 * ((size_t)L.s * L.W + L.w0)] = a0;
     B.part_c[2 * ((size_t)L.s * L.W + L.w0) + 1] = a1;
   }
+}
+
+// Inline replacement, per system (one block each): alpha of a running
+// recurrence, or the refinement decision of a system whose FP64 residual the
+// row kernel just recomputed -- marked in rep[s], so that this iteration's
+// update skips it and the check counts it without a stopping test.
+__global__ void __launch_bounds__(kBatchThreads) bil_alpha_kernel(BatchArgs B) {
+  __shared__ double sm[3 * kBatchWarps];
+  const int s = blockIdx.x;
+  PcgState& S = B.st[s];
+  PcgState& O = B.so[s];
+  const bool repl = batch_needs_check(B, s);
+  if (!repl && S.done) return;  // uniform in the block
+  double v[3];
+  block_segment_sum<3>(B.part_b, 3, s * B.nb, (s + 1) * B.nb, v, sm);
+  if (threadIdx.x != 0) return;
+  if (repl) {
+    outer_decide(B, S, O, v[0], v[1], B.delta, B.max_outer);
+    B.rep[s] = 1;
+    return;
+  }
+  S.pq = v[0];
+  double alpha;
+  if (!pcg_alpha(&S, &alpha)) {
+    S.done = 1;
+    S.flag = 2;
+    S.status = GB_BREAKDOWN;
+    O.done = 1;
+    O.flag = 2;
+    O.status = GB_BREAKDOWN;
+  }
+  S.spare1 = alpha;
+}
+
+// Stopping test of the updated systems; a system that paused at its inner
+// threshold stays counted (its replacement comes next), one that stopped on
+// maxit or breakdown is final.
+__global__ void __launch_bounds__(kBatchThreads)
+    bil_check_kernel(BatchArgs B, cudaGraphConditionalHandle cond, int has_cond) {
+  __shared__ double sm[2 * kBatchWarps];
+  __shared__ int was_rep;
+  const int s = blockIdx.x;
+  PcgState& S = B.st[s];
+  PcgState& O = B.so[s];
+  if (threadIdx.x == 0) was_rep = B.rep[s];
+  __syncthreads();
+  if (was_rep) {
+    if (threadIdx.x == 0) {
+      B.rep[s] = 0;
+      if (!S.done) atomicAdd(&B.nactive[0], 1);  // resumed
+    }
+  } else if (!S.done) {  // uniform in the block
+    double v[2];
+    block_segment_sum<2>(B.part_c, 2, B.sys_c[s], B.sys_c[s + 1], v, sm);
+    if (threadIdx.x == 0) {
+      pcg_check(&S, v[0], nullptr);
+      if (!S.done) {
+        S.rho_prev = S.rho;
+        S.rho = B.jacobi ? v[1] : v[0];
+        atomicAdd(&B.nactive[0], 1);
+      } else if (S.flag == 0 && !O.done) {
+        atomicAdd(&B.nactive[0], 1);
+      } else if (!O.done) {
+        O.done = 1;
+        O.flag = S.flag;
+        O.status = S.status;
+      }
+    }
+  }
+  batch_loop_decide(B, cond, has_cond);
 }
 
 // [count][n] -> [n][count] (to_il) or back, 64 rows per tile through shared
@@ -706,18 +797,26 @@ struct gb_batch_s {
   const int* bundles = nullptr;
   int nb = 0, nc = 0;
   int il_grid = 0;  // interleaved: blocks of every row kernel (nb = its warps)
+  int il_ugrid = 0; // interleaved: blocks of the update kernel (nc / count = its warps)
   int nbun = 0;     // interleaved: bundles of the shared matrix
   std::vector<void*> owned;  // device buffers freed with the batch
   int *row_off = nullptr, *bsys = nullptr, *sys_b = nullptr, *chunk_r0 = nullptr, *csys = nullptr,
       *sys_c = nullptr;
   double *b = nullptr, *x = nullptr, *r = nullptr, *w = nullptr, *p = nullptr, *q = nullptr;
   float* w32 = nullptr;  // interleaved only
+  int* rep = nullptr;    // interleaved only: [count] replacement marks
+  int il_inline = 0;     // this solve replaces residuals inside the loop
+  double delta = 0.0;    // its inner tolerance
+  int max_outer = 0;
   PcgState *st = nullptr, *so = nullptr, *st_h = nullptr;
   double *part_b = nullptr, *part_c = nullptr;
   unsigned* tk = nullptr;
   int* nactive = nullptr;
   LoopGraph loop[2];  // [FP64, split]
   int loop_maxit[2] = {-1, -1};
+  int loop_inline[2] = {-1, -1};  // with delta and max_outer: captured in the graph
+  double loop_delta[2] = {0.0, 0.0};
+  int loop_mo[2] = {-1, -1};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -780,6 +879,7 @@ int batch_buffers(gb_batch bt) {
   const size_t N = bt->N;
   for (double** v : {&bt->b, &bt->x, &bt->r, &bt->w, &bt->p, &bt->q}) GB_TRY(balloc(bt, v, N));
   if (bt->inter) GB_TRY(balloc(bt, &bt->w32, N));
+  if (bt->inter) GB_TRY(balloc(bt, &bt->rep, bt->count));
   GB_TRY(balloc(bt, &bt->st, bt->count));
   GB_TRY(balloc(bt, &bt->so, bt->count));
   GB_CUDA_TRY(cudaMallocHost(&bt->st_h, sizeof(PcgState) * 2 * bt->count));
@@ -830,6 +930,10 @@ BatchArgs batch_args(gb_batch bt, int maxit) {
   B.tk = bt->tk;
   B.nactive = bt->nactive;
   B.maxit = maxit;
+  B.il_inline = bt->il_inline;
+  B.rep = bt->rep;
+  B.delta = bt->delta;
+  B.max_outer = bt->max_outer;
   return B;
 }
 
@@ -869,12 +973,13 @@ int batch_body(gb_batch bt, int split, int maxit, cudaGraphConditionalHandle con
   BatchArgs B = batch_args(bt, maxit);
   if (split) B.w32 = bt->w32;
   if (bt->inter) {
-    const int G = bt->il_grid;
     if (split) il_rows<float, IL_PQ>(bt, B, bt->a32, cond, has_cond);
     else il_rows<double, IL_PQ>(bt, B, bt->a, cond, has_cond);
-    breduce_alpha_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B);
-    bil_update_kernel<<<G, kBatchThreads, 0, bt->s>>>(B);
-    breduce_check_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B, cond, has_cond);
+    if (B.il_inline) bil_alpha_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B);
+    else breduce_alpha_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B);
+    bil_update_kernel<<<bt->il_ugrid, kBatchThreads, 0, bt->s>>>(B);
+    if (B.il_inline) bil_check_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B, cond, has_cond);
+    else breduce_check_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B, cond, has_cond);
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
   }
@@ -907,7 +1012,8 @@ int batch_loop(gb_batch bt, int split, int maxit, int use_graph) {
     return GB_OK;
   }
   LoopGraph& lg = bt->loop[split];
-  if (!lg.exec || bt->loop_maxit[split] != maxit) {
+  if (!lg.exec || bt->loop_maxit[split] != maxit || bt->loop_inline[split] != bt->il_inline ||
+      bt->loop_delta[split] != bt->delta || bt->loop_mo[split] != bt->max_outer) {
     if (lg.exec) cudaGraphExecDestroy(lg.exec);
     if (lg.graph) cudaGraphDestroy(lg.graph);
     lg = LoopGraph();
@@ -937,6 +1043,9 @@ int batch_loop(gb_batch bt, int split, int maxit, int use_graph) {
     GB_CUDA_TRY(cudaGraphInstantiate(&lg.exec, g, 0));
     lg.graph = g;
     bt->loop_maxit[split] = maxit;
+    bt->loop_inline[split] = bt->il_inline;
+    bt->loop_delta[split] = bt->delta;
+    bt->loop_mo[split] = bt->max_outer;
   }
   GB_CUDA_TRY(cudaGraphLaunch(lg.exec, bt->s));
   return GB_OK;
@@ -974,6 +1083,11 @@ int batch_solve(gb_batch bt, const double* b, double* x, const gb_pcg_opts* opts
     GB_CUDA_TRY(cudaMemcpyAsync(bt->b, b, bytes, cudaMemcpyDeviceToDevice, bt->s));
     GB_CUDA_TRY(cudaMemcpyAsync(bt->x, x, bytes, cudaMemcpyDeviceToDevice, bt->s));
   }
+  // interleaved split precision replaces residuals inside the loop
+  bt->il_inline = bt->inter && split;
+  bt->delta = itol;
+  bt->max_outer = o.max_outer;
+  if (bt->il_inline) GB_CUDA_TRY(cudaMemsetAsync(bt->rep, 0, sizeof(int) * bt->count, bt->s));
   BatchArgs B = batch_args(bt, o.maxit);
   if (split) B.w32 = bt->w32;
   const int gb64 = grid_bundles((const void*)bresid_kernel, bt->nb, bt->count, bt->shared);
@@ -982,8 +1096,9 @@ int batch_solve(gb_batch bt, const double* b, double* x, const gb_pcg_opts* opts
   breduce_init_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B);
   batch_target_kernel<<<ceil_div(bt->count, 128), 128, 0, bt->s>>>(B);
   GB_CUDA_TRY(cudaGetLastError());
-  GB_TRY(batch_loop(bt, split, o.maxit, o.use_graph));
-  if (split) {
+  // the loop guard allows one extra pass per replacement
+  GB_TRY(batch_loop(bt, split, bt->il_inline ? o.maxit + o.max_outer + 1 : o.maxit, o.use_graph));
+  if (split && !bt->il_inline) {
     for (int round = 0; round < o.max_outer + 1; ++round) {
       GB_CUDA_TRY(cudaMemsetAsync(bt->nactive + 1, 0, sizeof(int), bt->s));
       if (bt->inter) il_rows<double, IL_REPLACE>(bt, B, bt->a, 0, 0);
@@ -1177,9 +1292,14 @@ extern "C" int gb_pcg_solve_multi(gb_system sys, int nrhs, const double* B, doub
                                              il_smem_bytes<double>());
       bt->il_grid = (int)std::max(1LL, std::min(cap, ((long long)bt->nbun + kBatchWarps - 1) / kBatchWarps));
       bt->nb = bt->il_grid * kBatchWarps;
-      bt->nc = bt->nb * nrhs;
+      const long long steps = ((long long)sys->n + 32 / nrhs - 1) / (32 / nrhs);
+      bt->il_ugrid = (int)std::max(
+          1LL, std::min((long long)device_sm_count() * occupancy_blocks((const void*)bil_update_kernel, kBatchThreads),
+                        (steps + kBatchWarps * kIlUpd - 1) / (kBatchWarps * kIlUpd)));
+      const int wu = bt->il_ugrid * kBatchWarps;
+      bt->nc = wu * nrhs;
       std::vector<int> sc(nrhs + 1);
-      for (int s = 0; s <= nrhs; ++s) sc[s] = s * bt->nb;
+      for (int s = 0; s <= nrhs; ++s) sc[s] = s * wu;
       if (rc == GB_OK) rc = bupload(bt, &bt->sys_c, sc);
     } else {
       bt->bundles = sys->plan.bundles;
