@@ -557,25 +557,45 @@ __global__ void __launch_bounds__(kBatchThreads)
         const int e1 = !v ? 0 : staged ? sia[i - r0 + 1] : __ldg(B.ia + i + 1) - j0;
         TA acc = TA(0);
         double acc64 = 0.0;  // inline replacement: FP64 A x
-        for (int e = e0; e < e1; e += kIlBatch) {
-          int cc[kIlBatch];
-          TA xv[kIlBatch];
+        if (staged && !anyrep) {
+          // common path, without branches: indices past the row's end are
+          // clamped to its last entry and multiplied by a zero coefficient
+          for (int e = e0; e < e1; e += kIlBatch) {
+            const int last = e1 - 1;
+            int cc[kIlBatch];
+            TA av[kIlBatch], xv[kIlBatch];
 #pragma unroll
-          for (int u = 0; u < kIlBatch; ++u)
-            cc[u] = e + u < e1 ? (staged ? sj[e + u] : __ldg(B.ja + j0 + e + u)) : -1;
-          if (!kInline || !rep) {
+            for (int u = 0; u < kIlBatch; ++u) {
+              const int eu = min(e + u, last);
+              cc[u] = sj[eu];
+              av[u] = e + u <= last ? sa[eu] : TA(0);
+            }
 #pragma unroll
-            for (int u = 0; u < kIlBatch; ++u) xv[u] = cc[u] >= 0 ? __ldg(xs + (size_t)cc[u] * C + L.s) : TA(0);
+            for (int u = 0; u < kIlBatch; ++u) xv[u] = __ldg(xs + (unsigned)(cc[u] * C + L.s));
+#pragma unroll
+            for (int u = 0; u < kIlBatch; ++u) acc = fma_rn(av[u], xv[u], acc);
+          }
+        } else {  // bundles read from global memory, or warps with a replacing lane
+          for (int e = e0; e < e1; e += kIlBatch) {
+            int cc[kIlBatch];
+            TA xv[kIlBatch];
 #pragma unroll
             for (int u = 0; u < kIlBatch; ++u)
-              if (cc[u] >= 0) acc = fma_rn(staged ? sa[e + u] : __ldg(a + j0 + e + u), xv[u], acc);
-          } else {
-            double xd[kIlBatch];
+              cc[u] = e + u < e1 ? (staged ? sj[e + u] : __ldg(B.ja + j0 + e + u)) : -1;
+            if (!kInline || !rep) {
 #pragma unroll
-            for (int u = 0; u < kIlBatch; ++u) xd[u] = cc[u] >= 0 ? __ldg(B.x + (size_t)cc[u] * C + L.s) : 0.0;
+              for (int u = 0; u < kIlBatch; ++u) xv[u] = cc[u] >= 0 ? __ldg(xs + (size_t)cc[u] * C + L.s) : TA(0);
 #pragma unroll
-            for (int u = 0; u < kIlBatch; ++u)
-              if (cc[u] >= 0) acc64 = fma_rn(__ldg(B.a + j0 + e + u), xd[u], acc64);
+              for (int u = 0; u < kIlBatch; ++u)
+                if (cc[u] >= 0) acc = fma_rn(staged ? sa[e + u] : __ldg(a + j0 + e + u), xv[u], acc);
+            } else {
+              double xd[kIlBatch];
+#pragma unroll
+              for (int u = 0; u < kIlBatch; ++u) xd[u] = cc[u] >= 0 ? __ldg(B.x + (size_t)cc[u] * C + L.s) : 0.0;
+#pragma unroll
+              for (int u = 0; u < kIlBatch; ++u)
+                if (cc[u] >= 0) acc64 = fma_rn(__ldg(B.a + j0 + e + u), xd[u], acc64);
+            }
           }
         }
         if (!v) continue;
