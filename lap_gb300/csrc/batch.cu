@@ -474,32 +474,29 @@ struct IlLane {
   }
 };
 
-// The row kernels walk the shared matrix's SpMV bundles (<= 32 rows, <=
-// kBundleNnz entries), one warp per bundle: the warp stages the bundle's
-// column indices, values and row starts in shared memory with coalesced
-// loads, then takes the bundle's rows R at a time, so a row's only dependent
-// global loads are its gathers (kIlBatch of them in flight).  A bundle of
-// one row longer than kBundleNnz is read from global memory by row group 0.
+// The row kernels walk the shared matrix's SpMV bundles (<= 32 rows), one
+// warp per bundle.  Lane t stages row t's entries in shared memory padded to
+// kIlSlots slots -- column offsets pre-multiplied by the right-hand-side
+// count, padding pointing at the row itself with a zero value -- so each row
+// then reads its indices and values with a few 16-byte shared loads and
+// issues its kIlSlots gathers without a branch.  A bundle with a row of more
+// than kIlSlots entries (or a single long row) is read from global memory.
 //
 // Split precision (il_inline): a system whose recurrence paused at its
 // inner threshold gets its FP64 residual in the next iteration's A w pass:
 // its lanes compute r = b - A x with the FP64 values and x while the other
 // lanes compute their FP32 products, so no system waits for the others to
-// pause.  Warps without such a lane take the FP32-only path.
-template <typename TA>
-constexpr size_t il_smem_bytes() {
-  return (size_t)kBatchWarps * (kBundleNnz * (sizeof(int) + sizeof(TA)) + (kBundleRows + 1) * sizeof(int));
-}
+// pause.  Warps with such a lane take the global-memory path.
+constexpr int kIlSlots = 8;
 
 template <typename TA, int MODE>
 __global__ void __launch_bounds__(kBatchThreads)
     bil_row_kernel(BatchArgs B, const TA* __restrict__ a, cudaGraphConditionalHandle cond, int has_cond) {
-  extern __shared__ __align__(16) unsigned char il_smem[];
+  __shared__ __align__(16) int s_col[kBatchWarps][kBundleRows * kIlSlots];
+  __shared__ __align__(16) TA s_val[kBatchWarps][kBundleRows * kIlSlots];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  TA* sa = reinterpret_cast<TA*>(il_smem) + (size_t)wid * kBundleNnz;
-  int* sj = reinterpret_cast<int*>(il_smem + (size_t)kBatchWarps * kBundleNnz * sizeof(TA)) + wid * kBundleNnz;
-  int* sia = reinterpret_cast<int*>(il_smem + (size_t)kBatchWarps * kBundleNnz * (sizeof(TA) + sizeof(int))) +
-             wid * (kBundleRows + 1);
+  int* sc = s_col[wid];
+  TA* sv = s_val[wid];
   const IlLane L(B);
   if (MODE == IL_PQ && has_cond && blockIdx.x == 0 && threadIdx.x == 0) {
     const unsigned g = atomicAdd(&B.tk[2], 1u) + 1u;  // loop guard
@@ -529,17 +526,21 @@ __global__ void __launch_bounds__(kBatchThreads)
   if (__any_sync(0xffffffffu, live || rep)) {
     for (int bb = L.w0; bb < B.nbun; bb += L.W) {
       const int r0 = __ldg(B.bundles + bb), r1 = __ldg(B.bundles + bb + 1);
-      const int j0 = __ldg(B.ia + r0), j1 = __ldg(B.ia + r1);
-      const bool staged = j1 - j0 <= kBundleNnz;  // uniform in the warp
-      if (staged) {
-        for (int e = lane; e < j1 - j0; e += 32) {
-          sj[e] = __ldg(B.ja + j0 + e);
-          sa[e] = __ldg(a + j0 + e);
+      bool wide = false;
+      if (lane < r1 - r0) {
+        const int row = r0 + lane, k0 = __ldg(B.ia + row), k1 = __ldg(B.ia + row + 1);
+        wide = k1 - k0 > kIlSlots;
+        if (!anyrep) {
+#pragma unroll
+          for (int u = 0; u < kIlSlots; ++u) {
+            const bool ok = k0 + u < k1;
+            sc[lane * kIlSlots + u] = (ok ? __ldg(B.ja + k0 + u) : row) * C;
+            sv[lane * kIlSlots + u] = ok ? __ldg(a + k0 + u) : TA(0);
+          }
         }
-        if (lane < r1 - r0) sia[lane] = __ldg(B.ia + r0 + lane) - j0;
-        if (lane == 0) sia[r1 - r0] = j1 - j0;  // end of the last row (r1 - r0 <= 32)
-        __syncwarp();
       }
+      const bool fast = !anyrep && !__any_sync(0xffffffffu, wide);  // uniform in the warp
+      __syncwarp();
       for (int i = r0 + L.sub; i - L.sub < r1; i += L.R) {
         const bool v = (live || rep) && i < r1;
         const size_t k = (size_t)(v ? i : 0) * C + L.s;
@@ -553,48 +554,48 @@ __global__ void __launch_bounds__(kBatchThreads)
           o0 = v ? B.b[k] : 0.0;
           o1 = v && B.jacobi && MODE != IL_REPORT ? B.d_r[i] : 0.0;
         }
-        const int e0 = !v ? 0 : staged ? sia[i - r0] : __ldg(B.ia + i) - j0;
-        const int e1 = !v ? 0 : staged ? sia[i - r0 + 1] : __ldg(B.ia + i + 1) - j0;
         TA acc = TA(0);
         double acc64 = 0.0;  // inline replacement: FP64 A x
-        if (staged && !anyrep) {
-          // common path, without branches: indices past the row's end are
-          // clamped to its last entry and multiplied by a zero coefficient
-          for (int e = e0; e < e1; e += kIlBatch) {
-            const int last = e1 - 1;
-            int cc[kIlBatch];
-            TA av[kIlBatch], xv[kIlBatch];
+        if (fast) {
+          if (v) {
+            const int t = (i - r0) * kIlSlots;
+            int cc[kIlSlots];
+            TA av[kIlSlots], xv[kIlSlots];
 #pragma unroll
-            for (int u = 0; u < kIlBatch; ++u) {
-              const int eu = min(e + u, last);
-              cc[u] = sj[eu];
-              av[u] = e + u <= last ? sa[eu] : TA(0);
+            for (int u = 0; u < kIlSlots; u += 4) {
+              const int4 c4 = *reinterpret_cast<const int4*>(sc + t + u);
+              cc[u] = c4.x;
+              cc[u + 1] = c4.y;
+              cc[u + 2] = c4.z;
+              cc[u + 3] = c4.w;
             }
 #pragma unroll
-            for (int u = 0; u < kIlBatch; ++u) xv[u] = __ldg(xs + (unsigned)(cc[u] * C + L.s));
+            for (int u = 0; u < kIlSlots; ++u) av[u] = sv[t + u];
 #pragma unroll
-            for (int u = 0; u < kIlBatch; ++u) acc = fma_rn(av[u], xv[u], acc);
+            for (int u = 0; u < kIlSlots; ++u) xv[u] = __ldg(xs + (unsigned)(cc[u] + L.s));
+#pragma unroll
+            for (int u = 0; u < kIlSlots; ++u) acc = fma_rn(av[u], xv[u], acc);
           }
-        } else {  // bundles read from global memory, or warps with a replacing lane
+        } else {
+          const int e0 = v ? __ldg(B.ia + i) : 0, e1 = v ? __ldg(B.ia + i + 1) : 0;
           for (int e = e0; e < e1; e += kIlBatch) {
             int cc[kIlBatch];
-            TA xv[kIlBatch];
 #pragma unroll
-            for (int u = 0; u < kIlBatch; ++u)
-              cc[u] = e + u < e1 ? (staged ? sj[e + u] : __ldg(B.ja + j0 + e + u)) : -1;
+            for (int u = 0; u < kIlBatch; ++u) cc[u] = e + u < e1 ? __ldg(B.ja + e + u) : -1;
             if (!kInline || !rep) {
+              TA xv[kIlBatch];
 #pragma unroll
               for (int u = 0; u < kIlBatch; ++u) xv[u] = cc[u] >= 0 ? __ldg(xs + (size_t)cc[u] * C + L.s) : TA(0);
 #pragma unroll
               for (int u = 0; u < kIlBatch; ++u)
-                if (cc[u] >= 0) acc = fma_rn(staged ? sa[e + u] : __ldg(a + j0 + e + u), xv[u], acc);
+                if (cc[u] >= 0) acc = fma_rn(__ldg(a + e + u), xv[u], acc);
             } else {
               double xd[kIlBatch];
 #pragma unroll
               for (int u = 0; u < kIlBatch; ++u) xd[u] = cc[u] >= 0 ? __ldg(B.x + (size_t)cc[u] * C + L.s) : 0.0;
 #pragma unroll
               for (int u = 0; u < kIlBatch; ++u)
-                if (cc[u] >= 0) acc64 = fma_rn(__ldg(B.a + j0 + e + u), xd[u], acc64);
+                if (cc[u] >= 0) acc64 = fma_rn(__ldg(B.a + e + u), xd[u], acc64);
             }
           }
         }
@@ -968,24 +969,9 @@ int grid_chunks(int nc) {
   return std::max(1, std::min(nc, device_sm_count() * occupancy_blocks((const void*)bupdate_kernel, kBatchThreads)));
 }
 
-// Interleaved row kernels: dynamic shared memory for the bundle staging.
 template <typename TA, int MODE>
 void il_rows(gb_batch bt, const BatchArgs& B, const TA* a, cudaGraphConditionalHandle cond, int has_cond) {
-  bil_row_kernel<TA, MODE><<<bt->il_grid, kBatchThreads, il_smem_bytes<TA>(), bt->s>>>(B, a, cond, has_cond);
-}
-template <typename TA, int MODE>
-int il_attr() {
-  GB_CUDA_TRY(cudaFuncSetAttribute((const void*)bil_row_kernel<TA, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)il_smem_bytes<TA>()));
-  return GB_OK;
-}
-int il_setup() {
-  GB_TRY((il_attr<double, IL_RESID>()));
-  GB_TRY((il_attr<double, IL_PQ>()));
-  GB_TRY((il_attr<float, IL_PQ>()));
-  GB_TRY((il_attr<double, IL_REPLACE>()));
-  GB_TRY((il_attr<double, IL_REPORT>()));
-  return GB_OK;
+  bil_row_kernel<TA, MODE><<<bt->il_grid, kBatchThreads, 0, bt->s>>>(B, a, cond, has_cond);
 }
 
 // One iteration of every live system.
@@ -1306,10 +1292,8 @@ extern "C" int gb_pcg_solve_multi(gb_system sys, int nrhs, const double* B, doub
       bt->inter = 1;
       bt->bundles = sys->plan.bundles;
       bt->nbun = sys->plan.nbundles;
-      rc = il_setup();
       const long long cap = (long long)device_sm_count() *
-                            occupancy_blocks((const void*)bil_row_kernel<double, IL_PQ>, kBatchThreads,
-                                             il_smem_bytes<double>());
+                            occupancy_blocks((const void*)bil_row_kernel<double, IL_PQ>, kBatchThreads);
       bt->il_grid = (int)std::max(1LL, std::min(cap, ((long long)bt->nbun + kBatchWarps - 1) / kBatchWarps));
       bt->nb = bt->il_grid * kBatchWarps;
       const long long steps = ((long long)sys->n + 32 / nrhs - 1) / (32 / nrhs);
