@@ -484,9 +484,9 @@ struct IlLane {
 //
 // Split precision (il_inline): a system whose recurrence paused at its
 // inner threshold gets its FP64 residual in the next iteration's A w pass:
-// its lanes compute r = b - A x with the FP64 values and x while the other
-// lanes compute their FP32 products, so no system waits for the others to
-// pause.  Warps with such a lane take the global-memory path.
+// its lanes compute r = b - A x with the FP64 values (staged beside the FP32
+// ones in such iterations) and x, while the other lanes compute their FP32
+// products, so no system waits for the others to pause.
 constexpr int kIlSlots = 8;
 
 template <typename TA, int MODE>
@@ -494,15 +494,17 @@ __global__ void __launch_bounds__(kBatchThreads)
     bil_row_kernel(BatchArgs B, const TA* __restrict__ a, cudaGraphConditionalHandle cond, int has_cond) {
   __shared__ __align__(16) int s_col[kBatchWarps][kBundleRows * kIlSlots];
   __shared__ __align__(16) TA s_val[kBatchWarps][kBundleRows * kIlSlots];
+  constexpr bool kInline = MODE == IL_PQ && sizeof(TA) == 4;
+  __shared__ __align__(16) double s_val64[kInline ? kBatchWarps : 1][kInline ? kBundleRows * kIlSlots : 1];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int* sc = s_col[wid];
   TA* sv = s_val[wid];
+  double* sv64 = s_val64[kInline ? wid : 0];
   const IlLane L(B);
   if (MODE == IL_PQ && has_cond && blockIdx.x == 0 && threadIdx.x == 0) {
     const unsigned g = atomicAdd(&B.tk[2], 1u) + 1u;  // loop guard
     if (g > (unsigned)B.maxit + 8u) set_cond(cond, true, false);
   }
-  constexpr bool kInline = MODE == IL_PQ && sizeof(TA) == 4;
   bool live = false, rep = false, first = false;
   double beta = 0.0;
   if (L.ok) {
@@ -530,16 +532,15 @@ __global__ void __launch_bounds__(kBatchThreads)
       if (lane < r1 - r0) {
         const int row = r0 + lane, k0 = __ldg(B.ia + row), k1 = __ldg(B.ia + row + 1);
         wide = k1 - k0 > kIlSlots;
-        if (!anyrep) {
 #pragma unroll
-          for (int u = 0; u < kIlSlots; ++u) {
-            const bool ok = k0 + u < k1;
-            sc[lane * kIlSlots + u] = (ok ? __ldg(B.ja + k0 + u) : row) * C;
-            sv[lane * kIlSlots + u] = ok ? __ldg(a + k0 + u) : TA(0);
-          }
+        for (int u = 0; u < kIlSlots; ++u) {
+          const bool ok = k0 + u < k1;
+          sc[lane * kIlSlots + u] = (ok ? __ldg(B.ja + k0 + u) : row) * C;
+          sv[lane * kIlSlots + u] = ok ? __ldg(a + k0 + u) : TA(0);
+          if (kInline && anyrep) sv64[lane * kIlSlots + u] = ok ? __ldg(B.a + k0 + u) : 0.0;
         }
       }
-      const bool fast = !anyrep && !__any_sync(0xffffffffu, wide);  // uniform in the warp
+      const bool fast = !__any_sync(0xffffffffu, wide);  // uniform in the warp
       __syncwarp();
       for (int i = r0 + L.sub; i - L.sub < r1; i += L.R) {
         const bool v = (live || rep) && i < r1;
@@ -569,12 +570,24 @@ __global__ void __launch_bounds__(kBatchThreads)
               cc[u + 2] = c4.z;
               cc[u + 3] = c4.w;
             }
+            if (!kInline || !rep) {
 #pragma unroll
-            for (int u = 0; u < kIlSlots; ++u) av[u] = sv[t + u];
+              for (int u = 0; u < kIlSlots; ++u) av[u] = sv[t + u];
 #pragma unroll
-            for (int u = 0; u < kIlSlots; ++u) xv[u] = __ldg(xs + (unsigned)(cc[u] + L.s));
+              for (int u = 0; u < kIlSlots; ++u) xv[u] = __ldg(xs + (unsigned)(cc[u] + L.s));
+              // an FP64 product costs a slot of the slow FP64 pipe: padding
+              // (zero values) is skipped there, the FP32 chain stays branch-free
 #pragma unroll
-            for (int u = 0; u < kIlSlots; ++u) acc = fma_rn(av[u], xv[u], acc);
+              for (int u = 0; u < kIlSlots; ++u)
+                if (sizeof(TA) == 4 || av[u] != TA(0)) acc = fma_rn(av[u], xv[u], acc);
+            } else {
+              double xd[kIlSlots];
+#pragma unroll
+              for (int u = 0; u < kIlSlots; ++u) xd[u] = __ldg(B.x + (unsigned)(cc[u] + L.s));
+#pragma unroll
+              for (int u = 0; u < kIlSlots; ++u)
+                if (sv64[t + u] != 0.0) acc64 = fma_rn(sv64[t + u], xd[u], acc64);
+            }
           }
         } else {
           const int e0 = v ? __ldg(B.ia + i) : 0, e1 = v ? __ldg(B.ia + i + 1) : 0;
