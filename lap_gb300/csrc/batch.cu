@@ -494,6 +494,7 @@ __global__ void __launch_bounds__(kBatchThreads)
     bil_row_kernel(BatchArgs B, const TA* __restrict__ a, cudaGraphConditionalHandle cond, int has_cond) {
   __shared__ __align__(16) int s_col[kBatchWarps][kBundleRows * kIlSlots];
   __shared__ __align__(16) TA s_val[kBatchWarps][kBundleRows * kIlSlots];
+  __shared__ int s_cnt[kBatchWarps][kBundleRows];  // entries of each staged row
   constexpr bool kInline = MODE == IL_PQ && sizeof(TA) == 4;
   __shared__ __align__(16) double s_val64[kInline ? kBatchWarps : 1][kInline ? kBundleRows * kIlSlots : 1];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -532,6 +533,7 @@ __global__ void __launch_bounds__(kBatchThreads)
       if (lane < r1 - r0) {
         const int row = r0 + lane, k0 = __ldg(B.ia + row), k1 = __ldg(B.ia + row + 1);
         wide = k1 - k0 > kIlSlots;
+        s_cnt[wid][lane] = k1 - k0;
 #pragma unroll
         for (int u = 0; u < kIlSlots; ++u) {
           const bool ok = k0 + u < k1;
@@ -559,7 +561,7 @@ __global__ void __launch_bounds__(kBatchThreads)
         double acc64 = 0.0;  // inline replacement: FP64 A x
         if (fast) {
           if (v) {
-            const int t = (i - r0) * kIlSlots;
+            const int t = (i - r0) * kIlSlots, cnt = s_cnt[wid][i - r0];
             int cc[kIlSlots];
             TA av[kIlSlots], xv[kIlSlots];
 #pragma unroll
@@ -575,18 +577,18 @@ __global__ void __launch_bounds__(kBatchThreads)
               for (int u = 0; u < kIlSlots; ++u) av[u] = sv[t + u];
 #pragma unroll
               for (int u = 0; u < kIlSlots; ++u) xv[u] = __ldg(xs + (unsigned)(cc[u] + L.s));
-              // an FP64 product costs a slot of the slow FP64 pipe: padding
-              // (zero values) is skipped there, the FP32 chain stays branch-free
+              // an FP64 product costs a slot of the slow FP64 pipe: padding is
+              // skipped there (integer test), the FP32 chain stays branch-free
 #pragma unroll
               for (int u = 0; u < kIlSlots; ++u)
-                if (sizeof(TA) == 4 || av[u] != TA(0)) acc = fma_rn(av[u], xv[u], acc);
+                if (sizeof(TA) == 4 || u < cnt) acc = fma_rn(av[u], xv[u], acc);
             } else {
               double xd[kIlSlots];
 #pragma unroll
               for (int u = 0; u < kIlSlots; ++u) xd[u] = __ldg(B.x + (unsigned)(cc[u] + L.s));
 #pragma unroll
               for (int u = 0; u < kIlSlots; ++u)
-                if (sv64[t + u] != 0.0) acc64 = fma_rn(sv64[t + u], xd[u], acc64);
+                if (u < cnt) acc64 = fma_rn(sv64[t + u], xd[u], acc64);
             }
           }
         } else {
