@@ -489,6 +489,34 @@ struct IlLane {
 // products, so no system waits for the others to pause.
 constexpr int kIlSlots = 8;
 
+// FP64 sum of the first N staged products of a row: exactly N gathers and
+// N FMAs, since every FP64 instruction -- predicated off or not -- takes a
+// slot of GB300's narrow FP64 pipe.
+template <int N>
+__device__ __forceinline__ double il_chain64(const int* sc_row, const double* sv_row, const double* __restrict__ x,
+                                             int s) {
+  double xv[N > 0 ? N : 1], acc = 0.0;
+#pragma unroll
+  for (int u = 0; u < N; ++u) xv[u] = __ldg(x + (unsigned)(sc_row[u] + s));
+#pragma unroll
+  for (int u = 0; u < N; ++u) acc = fma_rn(sv_row[u], xv[u], acc);
+  return acc;
+}
+__device__ __forceinline__ double il_row64(int cnt, const int* sc_row, const double* sv_row,
+                                           const double* __restrict__ x, int s) {
+  switch (cnt) {  // uniform in the warp when one row spans it (32 right-hand sides)
+    case 8: return il_chain64<8>(sc_row, sv_row, x, s);
+    case 7: return il_chain64<7>(sc_row, sv_row, x, s);
+    case 6: return il_chain64<6>(sc_row, sv_row, x, s);
+    case 5: return il_chain64<5>(sc_row, sv_row, x, s);
+    case 4: return il_chain64<4>(sc_row, sv_row, x, s);
+    case 3: return il_chain64<3>(sc_row, sv_row, x, s);
+    case 2: return il_chain64<2>(sc_row, sv_row, x, s);
+    case 1: return il_chain64<1>(sc_row, sv_row, x, s);
+    default: return 0.0;
+  }
+}
+
 template <typename TA, int MODE>
 __global__ void __launch_bounds__(kBatchThreads)
     bil_row_kernel(BatchArgs B, const TA* __restrict__ a, cudaGraphConditionalHandle cond, int has_cond) {
@@ -562,33 +590,28 @@ __global__ void __launch_bounds__(kBatchThreads)
         if (fast) {
           if (v) {
             const int t = (i - r0) * kIlSlots, cnt = s_cnt[wid][i - r0];
-            int cc[kIlSlots];
-            TA av[kIlSlots], xv[kIlSlots];
+            if constexpr (sizeof(TA) == 8) {
+              acc = il_row64(cnt, sc + t, sv + t, xs, L.s);
+            } else if (!kInline || !rep) {
+              // FP32: all slots, padding included, without a branch
+              int cc[kIlSlots];
+              TA av[kIlSlots], xv[kIlSlots];
 #pragma unroll
-            for (int u = 0; u < kIlSlots; u += 4) {
-              const int4 c4 = *reinterpret_cast<const int4*>(sc + t + u);
-              cc[u] = c4.x;
-              cc[u + 1] = c4.y;
-              cc[u + 2] = c4.z;
-              cc[u + 3] = c4.w;
-            }
-            if (!kInline || !rep) {
+              for (int u = 0; u < kIlSlots; u += 4) {
+                const int4 c4 = *reinterpret_cast<const int4*>(sc + t + u);
+                cc[u] = c4.x;
+                cc[u + 1] = c4.y;
+                cc[u + 2] = c4.z;
+                cc[u + 3] = c4.w;
+              }
 #pragma unroll
               for (int u = 0; u < kIlSlots; ++u) av[u] = sv[t + u];
 #pragma unroll
               for (int u = 0; u < kIlSlots; ++u) xv[u] = __ldg(xs + (unsigned)(cc[u] + L.s));
-              // an FP64 product costs a slot of the slow FP64 pipe: padding is
-              // skipped there (integer test), the FP32 chain stays branch-free
 #pragma unroll
-              for (int u = 0; u < kIlSlots; ++u)
-                if (sizeof(TA) == 4 || u < cnt) acc = fma_rn(av[u], xv[u], acc);
+              for (int u = 0; u < kIlSlots; ++u) acc = fma_rn(av[u], xv[u], acc);
             } else {
-              double xd[kIlSlots];
-#pragma unroll
-              for (int u = 0; u < kIlSlots; ++u) xd[u] = __ldg(B.x + (unsigned)(cc[u] + L.s));
-#pragma unroll
-              for (int u = 0; u < kIlSlots; ++u)
-                if (u < cnt) acc64 = fma_rn(sv64[t + u], xd[u], acc64);
+              acc64 = il_row64(cnt, sc + t, sv64 + t, B.x, L.s);
             }
           }
         } else {
