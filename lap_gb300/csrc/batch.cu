@@ -313,6 +313,12 @@ __device__ __forceinline__ bool batch_needs_check(const BatchArgs& B, int s) {
   return B.st[s].done && B.st[s].flag == 0 && !B.so[s].done;
 }
 
+// Inline replacement: the paused systems are replaced together in a pass
+// opened by the loop's decision (nactive[3]), see bil_check_kernel.
+__device__ __forceinline__ bool il_replaces(const BatchArgs& B, int s) {
+  return B.il_inline && *(volatile int*)&B.nactive[3] && batch_needs_check(B, s);
+}
+
 __global__ void __launch_bounds__(kBatchThreads) btrue_kernel(BatchArgs B, int replace) {
   __shared__ double stage[kBatchWarps][kBundleNnz];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -543,7 +549,7 @@ __global__ void __launch_bounds__(kBatchThreads)
       live = !S.done;
       first = S.iter == 0;
       beta = first ? 0.0 : S.rho / S.rho_prev;
-      if (kInline && B.il_inline) rep = batch_needs_check(B, L.s);
+      if (kInline) rep = il_replaces(B, L.s);
     }
     if (MODE == IL_REPLACE) live = batch_needs_check(B, L.s);
   }
@@ -740,7 +746,7 @@ __global__ void __launch_bounds__(kBatchThreads) bil_alpha_kernel(BatchArgs B) {
   const int s = blockIdx.x;
   PcgState& S = B.st[s];
   PcgState& O = B.so[s];
-  const bool repl = batch_needs_check(B, s);
+  const bool repl = il_replaces(B, s);
   if (!repl && S.done) return;  // uniform in the block
   double v[3];
   block_segment_sum<3>(B.part_b, 3, s * B.nb, (s + 1) * B.nb, v, sm);
@@ -764,8 +770,14 @@ __global__ void __launch_bounds__(kBatchThreads) bil_alpha_kernel(BatchArgs B) {
 }
 
 // Stopping test of the updated systems; a system that paused at its inner
-// threshold stays counted (its replacement comes next), one that stopped on
-// maxit or breakdown is final.
+// threshold stays counted (nactive[1] counts those waiting), one that
+// stopped on maxit or breakdown is final.  The last block opens a
+// replacement pass for all waiting systems (nactive[3]) once all running
+// systems have paused, a quarter of the live ones wait, or the first has
+// waited kIlWait iterations: each pass costs the whole grid FP64 products,
+// so paused systems share one.
+constexpr int kIlWait = 4;
+
 __global__ void __launch_bounds__(kBatchThreads)
     bil_check_kernel(BatchArgs B, cudaGraphConditionalHandle cond, int has_cond) {
   __shared__ double sm[2 * kBatchWarps];
@@ -791,12 +803,34 @@ __global__ void __launch_bounds__(kBatchThreads)
         atomicAdd(&B.nactive[0], 1);
       } else if (S.flag == 0 && !O.done) {
         atomicAdd(&B.nactive[0], 1);
+        atomicAdd(&B.nactive[1], 1);
       } else if (!O.done) {
         O.done = 1;
         O.flag = S.flag;
         O.status = S.status;
       }
     }
+  } else if (threadIdx.x == 0 && S.flag == 0 && !O.done) {  // still waiting for its pass
+    atomicAdd(&B.nactive[0], 1);
+    atomicAdd(&B.nactive[1], 1);
+  }
+  // the last block: the next pass, then the loop's decision
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(&B.tk[1], 1u) == gridDim.x - 1u;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    B.tk[1] = 0u;
+    const int waiting = atomicExch(&B.nactive[1], 0);
+    const int live = *(volatile int*)&B.nactive[0];
+    const unsigned waited = waiting > 0 ? B.tk[3] + 1u : 0u;
+    const bool go = waiting > 0 && (waiting == live || 4 * waiting >= live || waited >= (unsigned)kIlWait);
+    B.nactive[3] = go ? 1 : 0;
+    B.tk[3] = go ? 0u : waited;
+    __threadfence();
   }
   batch_loop_decide(B, cond, has_cond);
 }
@@ -1140,8 +1174,8 @@ int batch_solve(gb_batch bt, const double* b, double* x, const gb_pcg_opts* opts
   breduce_init_kernel<<<grid_sys(bt->count), kBatchThreads, 0, bt->s>>>(B);
   batch_target_kernel<<<ceil_div(bt->count, 128), 128, 0, bt->s>>>(B);
   GB_CUDA_TRY(cudaGetLastError());
-  // the loop guard allows one extra pass per replacement
-  GB_TRY(batch_loop(bt, split, bt->il_inline ? o.maxit + o.max_outer + 1 : o.maxit, o.use_graph));
+  // the loop guard allows a replacement pass and its wait per replacement
+  GB_TRY(batch_loop(bt, split, bt->il_inline ? o.maxit + o.max_outer * (kIlWait + 1) + 1 : o.maxit, o.use_graph));
   if (split && !bt->il_inline) {
     for (int round = 0; round < o.max_outer + 1; ++round) {
       GB_CUDA_TRY(cudaMemsetAsync(bt->nactive + 1, 0, sizeof(int), bt->s));
