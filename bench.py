@@ -262,6 +262,49 @@ def run_workload(args, local):
                     x_rel_err_vs_reference=float(np.linalg.norm(x.cpu().numpy() - ref["x"]) /
                                                  np.linalg.norm(ref["x"])),
                     cpu_reference_ms=ref["solve_s"] * 1e3, cpu_cores=1)
+    elif wl == "mmread128":
+        import ctypes as C
+        import tempfile
+
+        A, _ = gen.grid3d_lognormal(128, seed=1002)
+        line["config"] = ("128^3 lognormal Laplacian written as 'coordinate real symmetric' (lower triangle, "
+                          "%.17g values), read into CSR: host read_mm_file + coo_to_csr vs gb_mm_read_csr")
+        with tempfile.TemporaryDirectory() as td:
+            path = os.path.join(td, "g128.mtx")
+            tw = time.time()
+            gen.write_mm(path, A)
+            line["file_bytes"] = os.path.getsize(path)
+            line["write_s"] = round(time.time() - tw, 1)
+            L = gb.lib()
+            gb.read_mm_device(path)  # warm-up (module load, first allocations)
+            runs = []
+            for _ in range(3):
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                ia, ja, a, info = gb.read_mm_device(path)
+                runs.append((time.perf_counter() - t1, info))
+            wall, info = min(runs, key=lambda t: t[0])
+            line["device"] = {"wall_ms": round(wall * 1e3, 1), "read_ms": round(info["read_ms"], 1),
+                              "h2d_ms": round(info["h2d_ms"], 2), "device_ms": round(info["device_ms"], 2),
+                              "device_gbs_of_file": round(line["file_bytes"] / info["device_ms"] / 1e6, 1),
+                              "host_parsed": info["host_parsed"], "nnz": info["nnz"]}
+            M = gb.MMatrix()
+            t1 = time.perf_counter()
+            L.read_mm_file(path.encode(), C.byref(M))
+            L.coo_to_csr(C.byref(M))
+            line["host_reader_ms"] = round((time.perf_counter() - t1) * 1e3, 1)
+            hia = np.ctypeslib.as_array(M.csr_ia, (M.n + 1,)).copy()
+            hja = np.ctypeslib.as_array(M.csr_ja, (M.nnz_unpacked,)).copy()
+            ha = np.ctypeslib.as_array(M.csr_vals, (M.nnz_unpacked,)).copy()
+            libc = C.CDLL(None)
+            for q in (M.csr_ia, M.csr_ja, M.csr_vals):
+                libc.free(C.cast(q, C.c_void_p))
+            line["identical_to_host_reader"] = bool(
+                np.array_equal(ia.cpu().numpy(), hia) and np.array_equal(ja.cpu().numpy(), hja)
+                and np.array_equal(a.cpu().numpy().view(np.int64), ha.view(np.int64)))
+            line["identical_to_generator"] = bool(
+                np.array_equal(hia, A.ia) and np.array_equal(hja, A.ja) and np.array_equal(ha, A.a))
+            line["speedup_vs_host_reader"] = round(line["host_reader_ms"] / (wall * 1e3), 1)
     elif wl == "chunglu4m":
         A, b = gen.chung_lu(1 << 22, seed=1003)
         line["config"] = f"Chung-Lu n={A.n} nnz={A.nnz}, A=1.001 D - W, ichol, tol 1e-10"
@@ -496,7 +539,8 @@ def main():
                     help="only the eager per-kernel profile of each precision mode (for ncu)")
     ap.add_argument("--profile-iters", type=int, default=3)
     ap.add_argument("--workload", default="ichol128",
-                    choices=["ichol128", "jacobi256", "chunglu4m", "batch512", "multirhs32", "adjoint1024"],
+                    choices=["ichol128", "jacobi256", "chunglu4m", "batch512", "multirhs32", "adjoint1024",
+                             "mmread128"],
                     help="ichol128 is the headline line; the others are the remaining configurations")
     ap.add_argument("--fd-edges", type=int, default=16)
     args = ap.parse_args()

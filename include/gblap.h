@@ -207,6 +207,37 @@ int gb_profile_iteration(gb_system sys, const double *b, double *x, int precisio
  * n only (fixed chunking), and may differ from cuda_dot() in the last bits. */
 int gb_dot_noalloc(int n, const double *v, const double *w, double *result_host, void *stream);
 
+/* ------------------------------------------------------------ Matrix Market on the device */
+/* A CSR matrix built on the device from a Matrix Market coordinate file.
+ * ia [n+1], ja [nnz], a [nnz] are device arrays owned by the caller (free
+ * them with gb_mm_csr_free). */
+typedef struct {
+  int n, m;              /* rows, columns (size line) */
+  long long nnz_file;    /* entries the size line announces */
+  int nnz;               /* CSR entries: a symmetric file's off-diagonal entries mirrored */
+  int symmetric, pattern;
+  int *ia, *ja;
+  double *a;
+  int host_parsed;       /* values outside the device's exact decimal path, parsed by strtod */
+  double read_ms;        /* host file read (gb_mm_read_csr) */
+  double h2d_ms;         /* the bytes' copy to the device */
+  double device_ms;      /* line split, parse, mirror, sort and CSR build */
+} gb_mm_csr;
+
+/* read_mm_file (io_utils.c:15-74) followed by coo_to_csr (io_utils.c:141-235),
+ * with the same CSR bit for bit, built on the device: the host reads the file
+ * and its header, the bytes are copied once, and line splitting, number
+ * parsing (values rounded to the nearest double exactly, as strtod does),
+ * symmetric mirroring and the column sort run as device kernels.  Lines
+ * starting with '%' and blank lines are skipped; entries past the size line's
+ * count are ignored.  GB_BAD_INPUT for a missing size line, a malformed or
+ * out-of-range entry, or fewer entries than announced; GB_NOT_SUPPORTED for
+ * sizes past int32. */
+int gb_mm_read_csr(const char *path, gb_mm_csr *out);
+/* The same from the whole file held in host memory. */
+int gb_mm_parse_csr(const char *bytes, long long len, gb_mm_csr *out);
+int gb_mm_csr_free(gb_mm_csr *m);
+
 #ifdef __cplusplus
 }
 #endif

@@ -68,6 +68,16 @@ class MMatrix(C.Structure):
                 ("symmetric", C.c_int)]
 
 
+class MmCsr(C.Structure):
+    """gb_mm_csr (include/gblap.h): a CSR matrix built on the device from a
+    Matrix Market file."""
+    _fields_ = [("n", C.c_int), ("m", C.c_int), ("nnz_file", C.c_longlong), ("nnz", C.c_int),
+                ("symmetric", C.c_int), ("pattern", C.c_int),
+                ("ia", C.c_void_p), ("ja", C.c_void_p), ("a", C.c_void_p),
+                ("host_parsed", C.c_int), ("read_ms", C.c_double), ("h2d_ms", C.c_double),
+                ("device_ms", C.c_double)]
+
+
 def _proto(L: C.CDLL) -> None:
     vp, i, d = C.c_void_p, C.c_int, C.c_double
     sig = {
@@ -93,6 +103,9 @@ def _proto(L: C.CDLL) -> None:
         "gb_autotune_spmv": (i, [vp, C.POINTER(i)]),
         "gb_debug_set_spin_budget": (i, [vp, C.c_ulonglong]),
         "gb_dot_noalloc": (i, [i, vp, vp, C.POINTER(C.c_double), vp]),
+        "gb_mm_read_csr": (i, [C.c_char_p, C.POINTER(MmCsr)]),
+        "gb_mm_parse_csr": (i, [C.c_char_p, C.c_longlong, C.POINTER(MmCsr)]),
+        "gb_mm_csr_free": (i, [C.POINTER(MmCsr)]),
         "gb_profile_iteration": (i, [vp, vp, vp, i, i, C.c_char_p, i, vp, vp, i, C.POINTER(i)]),
         # LAP surface
         "cuda_dot": (d, [i, vp, vp]),
@@ -357,6 +370,40 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def read_mm_device(path=None, data: bytes | None = None):
+    """A Matrix Market coordinate file (``path``, or its bytes ``data``) parsed
+    into CSR on the device (gb_mm_read_csr / gb_mm_parse_csr).  Returns
+    (ia, ja, a) as CUDA tensors and an info dict (sizes, flags, timings)."""
+    import torch
+
+    out = MmCsr()
+    if data is not None:
+        rc = lib().gb_mm_parse_csr(data, len(data), C.byref(out))
+    else:
+        rc = lib().gb_mm_read_csr(os.fsencode(path), C.byref(out))
+    check(rc, "gb_mm_read_csr")
+    try:
+        ia = torch.empty(out.n + 1, dtype=torch.int32, device="cuda")
+        ja = torch.empty(max(out.nnz, 0), dtype=torch.int32, device="cuda")
+        a = torch.empty(max(out.nnz, 0), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        _copy_dev(ia, out.ia, out.n + 1, 4)
+        if out.nnz:
+            _copy_dev(ja, out.ja, out.nnz, 4)
+            _copy_dev(a, out.a, out.nnz, 8)
+    finally:
+        lib().gb_mm_csr_free(C.byref(out))
+    info = {k: getattr(out, k) for k in ("n", "m", "nnz_file", "nnz", "symmetric", "pattern", "host_parsed",
+                                         "read_ms", "h2d_ms", "device_ms")}
+    return ia, ja, a, info
+
+
+def _copy_dev(dst, src_ptr, count, size):
+    """Device-to-device copy of count elements of size bytes from a raw device
+    pointer into a tensor (devMem's memcpyDevice)."""
+    lib().memcpyDevice(C.c_void_p(dst.data_ptr()), C.c_void_p(src_ptr), count, size, b"D2D")
 
 
 def solve_multi(system, B, X=None, **kw):

@@ -22,7 +22,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgblap.so")
 
 SOURCES = ["kernels.cu", "sptrsv.cu", "tri_plan.cu", "pcg.cu", "precond.cu", "system.cu", "lap_abi.cu",
-           "lap_host.cu", "extras.cu", "batch.cu", "noalloc.cu"]
+           "lap_host.cu", "extras.cu", "batch.cu", "noalloc.cu", "mmio.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

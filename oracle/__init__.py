@@ -192,3 +192,80 @@ def ref_solve(n, ia, ja, a, b, prec="line_jacobi", tol=1e-8, maxit=10000, M=1, K
     it = L.ref_solve_csr(n, len(ja), ia, ja, a, bb, x, prec.encode(), tol, maxit, M, K,
                          C.byref(flag), hist, None, None)
     return dict(x=x, iters=it, flag=flag.value, res_hist=hist[: it + 1].copy())
+
+
+# ---------------------------------------------------------------- Matrix Market
+_NUM_PREFIX = None
+
+
+def _strtod_prefix(tok: str) -> float:
+    """The value strtod reads from the start of ``tok`` (sscanf's %lf): the
+    longest decimal (or inf / nan) prefix, correctly rounded as glibc does --
+    Python's float() rounds decimals the same way."""
+    global _NUM_PREFIX
+    import re
+
+    if _NUM_PREFIX is None:
+        _NUM_PREFIX = re.compile(r"[+-]?(?:inf(?:inity)?|nan|(?:\d+\.?\d*|\.\d+)(?:[eE][+-]?\d+)?)", re.I)
+    m = _NUM_PREFIX.match(tok)
+    if not m:
+        raise ValueError(f"no number in {tok!r}")
+    return float(m.group(0))
+
+
+def mm_csr(data: bytes):
+    """read_mm_file (io_utils.c:15-74) + coo_to_csr (io_utils.c:141-235) on
+    the bytes of a Matrix Market coordinate file, restated in Python/numpy.
+
+    Banner flags 'pattern' / 'symmetric' (io_utils.c:24-35), '%' comment
+    lines and the size line (:37-44); one entry per data line "r c [v]",
+    1-based (:55-70), where this restatement skips '%' and blank lines and
+    stops at the announced count; a symmetric file's off-diagonal entries
+    mirrored (:150-157, :177-194); rows bucketed in encounter order, then each
+    row sorted by column with equal columns kept in that order (:199-210, the
+    reference's qsort being glibc's merge sort here).
+    Returns (n, m, symmetric, ia, ja, a)."""
+    text = data.decode("ascii", errors="replace")
+    lines = text.split("\n")
+    banner = lines[0]
+    pattern = "pattern" in banner
+    symmetric = "symmetric" in banner
+    k = 1
+    while k < len(lines) and lines[k].startswith("%"):
+        k += 1
+    n, m, nnz = (int(t) for t in lines[k].split()[:3])
+    rows, cols, vals = [], [], []
+    for line in lines[k + 1:]:
+        if len(rows) == nnz:
+            break
+        s = line.strip(" \t\r")
+        if not s or s.startswith("%"):
+            continue
+        parts = s.split()
+        r, c = int(parts[0]), int(parts[1])
+        if not (1 <= r <= n and 1 <= c <= m):
+            raise ValueError(f"entry out of range: {s!r}")
+        rows.append(r - 1)
+        cols.append(c - 1)
+        vals.append(1.0 if pattern else _strtod_prefix(parts[2]))
+    if len(rows) < nnz:
+        raise ValueError(f"file ended after {len(rows)} of {nnz} entries")
+    r = np.array(rows, dtype=np.int64)
+    c = np.array(cols, dtype=np.int64)
+    v = np.array(vals, dtype=np.float64)
+    if symmetric:
+        off = r != c
+        # encounter order: each entry, then its mirror
+        er = np.empty(2 * len(r), dtype=np.int64)
+        ec = np.empty_like(er)
+        ev = np.empty(2 * len(r))
+        keep = np.ones(2 * len(r), dtype=bool)
+        er[0::2], ec[0::2], ev[0::2] = r, c, v
+        er[1::2], ec[1::2], ev[1::2] = c, r, v
+        keep[1::2] = off
+        r, c, v = er[keep], ec[keep], ev[keep]
+    order = np.lexsort((c, r))  # stable: ties keep encounter order
+    r, c, v = r[order], c[order], v[order]
+    ia = np.zeros(n + 1, dtype=np.int32)
+    np.cumsum(np.bincount(r, minlength=n), out=ia[1:])
+    return n, m, symmetric, ia, c.astype(np.int32), v

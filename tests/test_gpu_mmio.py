@@ -1,0 +1,102 @@
+"""Matrix Market -> CSR on the device (gb_mm_read_csr / gb_mm_parse_csr)
+against the oracle's restatement of read_mm_file + coo_to_csr, itself pinned
+to the reference's reader (tests/test_oracle.py): ia, ja and the values'
+bit patterns must be identical."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a GPU", allow_module_level=True)
+
+import lap_gb300 as gb  # noqa: E402
+import mm_cases  # noqa: E402
+import oracle  # noqa: E402
+from conftest import ROOT  # noqa: E402
+from lap_gb300 import gen  # noqa: E402
+
+
+def _same(text_or_bytes, **kw):
+    data = text_or_bytes if isinstance(text_or_bytes, bytes) else text_or_bytes.encode()
+    ia, ja, a, info = gb.read_mm_device(data=data)
+    n, m, sym, oia, oja, oa = oracle.mm_csr(data)
+    assert (info["n"], info["m"], bool(info["symmetric"])) == (n, m, sym)
+    assert np.array_equal(ia.cpu().numpy(), oia)
+    assert np.array_equal(ja.cpu().numpy(), oja)
+    got = a.cpu().numpy()
+    bad = np.nonzero(got.view(np.int64) != oa.view(np.int64))[0]
+    assert bad.size == 0, (bad[:5], got[bad[:5]], oa[bad[:5]])
+    return info
+
+
+def test_reference_fixture(golden):
+    """grid6.mtx against the CSR the reference's own reader produced."""
+    path = f"{ROOT}/tests/golden/grid6.mtx"
+    ia, ja, a, info = gb.read_mm_device(path)
+    assert info["symmetric"] == 1 and info["n"] == 36 and info["host_parsed"] == 0
+    assert np.array_equal(ia.cpu().numpy(), golden["mm_ia"])
+    assert np.array_equal(ja.cpu().numpy(), golden["mm_ja"])
+    assert np.array_equal(a.cpu().numpy().view(np.int64), golden["mm_a"].view(np.int64))
+
+
+@pytest.mark.parametrize("kind", ["general", "symmetric", "pattern", "comments"])
+def test_stress_texts(kind):
+    text = {"general": mm_cases.general_text(), "symmetric": mm_cases.symmetric_text(),
+            "pattern": mm_cases.pattern_text(),
+            "comments": mm_cases.with_comments_and_blanks(mm_cases.general_text(seed=5))}[kind]
+    info = _same(text)
+    if kind == "general":
+        assert info["host_parsed"] > 0  # the spellings outside the exact path went to strtod
+
+
+def test_values_round_like_strtod():
+    """200k random spellings (repr, %.17g, %.6e, %g, integers, 1-19 digit
+    mantissas with exponents in [-40, 40]): every value's bits equal
+    Python's correctly rounded float(), which is what strtod returns."""
+    rng = np.random.default_rng(7)
+    vals = mm_cases.value_strings(rng, 200_000)
+    n = 1000
+    lines = ["%%MatrixMarket matrix coordinate real general", f"{n} {n} {len(vals)}"]
+    r = rng.integers(1, n + 1, len(vals))
+    c = rng.integers(1, n + 1, len(vals))
+    lines += [f"{r[i]} {c[i]} {v}" for i, v in enumerate(vals)]
+    info = _same("\n".join(lines) + "\n")
+    assert info["host_parsed"] < 0.2 * len(vals)
+
+
+def test_generated_laplacian_file(tmp_path):
+    """A 12^3 lognormal Laplacian written as the benchmark writes its files."""
+    A, _ = gen.grid3d_lognormal(12, seed=1002)
+    p = tmp_path / "g12.mtx"
+    gen.write_mm(str(p), A)
+    ia, ja, a, info = gb.read_mm_device(str(p))
+    assert info["host_parsed"] == 0 and info["nnz"] == len(A.ja)
+    assert np.array_equal(ia.cpu().numpy(), A.ia) and np.array_equal(ja.cpu().numpy(), A.ja)
+    assert np.array_equal(a.cpu().numpy(), A.a)  # %.17g round-trips exactly
+    _same(p.read_bytes())
+
+
+def test_edge_cases():
+    # no entries
+    ia, ja, a, info = gb.read_mm_device(data=b"%%MatrixMarket matrix coordinate real general\n3 3 0\n")
+    assert info["nnz"] == 0 and ia.cpu().tolist() == [0, 0, 0, 0]
+    # extra lines past the announced count are ignored
+    _same("%%MatrixMarket matrix coordinate real general\n2 2 1\n1 2 3.5\n2 1 4.5\n")
+    # a single entry with no newline at the end; a diagonal-only symmetric file
+    _same("%%MatrixMarket matrix coordinate real symmetric\n1 1 1\n1 1 -2.5")
+    # empty rows
+    _same("%%MatrixMarket matrix coordinate real general\n5 5 2\n5 1 1\n1 5 2\n")
+
+
+@pytest.mark.parametrize("text", [
+    "%%MatrixMarket matrix coordinate real general\n",                       # no size line
+    "%%MatrixMarket matrix coordinate real general\n2 2 2\n1 1 1.0\n",       # fewer entries
+    "%%MatrixMarket matrix coordinate real general\n2 2 1\n3 1 1.0\n",       # row out of range
+    "%%MatrixMarket matrix coordinate real general\n2 2 1\n1 0 1.0\n",       # column 0
+    "%%MatrixMarket matrix coordinate real general\n2 2 1\n1 x 1.0\n",       # not a number
+])
+def test_rejects_bad_files(text):
+    with pytest.raises(gb.GbError):
+        gb.read_mm_device(data=text.encode())

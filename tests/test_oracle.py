@@ -111,3 +111,42 @@ def test_reference_library_agrees_when_built(golden):
         r1 = oracle.solve(A.n, A.ia, A.ja, A.a, b, prec, 1e-9, 3000)
         assert r0["iters"] == r1["iters"]
         assert np.array_equal(r0["x"], r1["x"])
+
+
+# ---------------------------------------------------------------- Matrix Market
+def test_mm_csr_oracle_matches_reference_fixture(golden):
+    """oracle.mm_csr (read_mm_file + coo_to_csr restated) against the CSR the
+    reference's own reader produced for grid6.mtx."""
+    with open(os.path.join(ROOT, "tests", "golden", "grid6.mtx"), "rb") as f:
+        n, m, sym, ia, ja, a = oracle.mm_csr(f.read())
+    assert (n, m, sym) == (36, 36, True)
+    assert np.array_equal(ia, golden["mm_ia"]) and np.array_equal(ja, golden["mm_ja"])
+    assert np.array_equal(a.view(np.int64), golden["mm_a"].view(np.int64))
+
+
+@pytest.mark.parametrize("kind", ["general", "symmetric", "pattern"])
+def test_mm_csr_oracle_matches_reference_reader(kind, tmp_path):
+    """The same against the reference's compiled reader on harder texts:
+    duplicates, CRLF ends, tabs, every value spelling of tests/mm_cases.py
+    (skipped where the reference was not compiled)."""
+    import mm_cases
+
+    L = oracle.ref_lib()
+    if L is None:
+        pytest.skip("reference library not built here")
+    text = {"general": mm_cases.general_text, "symmetric": mm_cases.symmetric_text,
+            "pattern": mm_cases.pattern_text}[kind]()
+    p = tmp_path / f"{kind}.mtx"
+    p.write_text(text)
+    L.ref_read_mm_csr.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                  C.POINTER(C.POINTER(C.c_int)), C.POINTER(C.POINTER(C.c_int)),
+                                  C.POINTER(C.POINTER(C.c_double))]
+    n, nnz = C.c_int(), C.c_int()
+    pia, pja, pa = C.POINTER(C.c_int)(), C.POINTER(C.c_int)(), C.POINTER(C.c_double)()
+    L.ref_read_mm_csr(str(p).encode(), C.byref(n), C.byref(nnz), C.byref(pia), C.byref(pja), C.byref(pa))
+    ia = np.ctypeslib.as_array(pia, (n.value + 1,)).copy()
+    ja = np.ctypeslib.as_array(pja, (nnz.value,)).copy()
+    a = np.ctypeslib.as_array(pa, (nnz.value,)).copy()
+    _, _, _, oia, oja, oa = oracle.mm_csr(text.encode())
+    assert np.array_equal(ia, oia) and np.array_equal(ja, oja)
+    assert np.array_equal(a.view(np.int64), oa.view(np.int64))
