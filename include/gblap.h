@@ -238,6 +238,26 @@ int gb_mm_read_csr(const char *path, gb_mm_csr *out);
 int gb_mm_parse_csr(const char *bytes, long long len, gb_mm_csr *out);
 int gb_mm_csr_free(gb_mm_csr *m);
 
+/* The Laplacian driver's setup (cg_driver.c:38-45) on the device:
+ * read_adjacency_file (io_utils.c:82-138: the file's entries, symmetric
+ * whatever the banner says, plus one unit diagonal entry per vertex),
+ * coo_to_csr, then create_L_and_split's in-place Laplacian
+ * (io_utils.c:367-491): weighted = 0 gives D - W, weighted = 1 gives
+ * I - D^-1/2 W D^-1/2.  The reference sums each degree into an int, so
+ * every partial sum of a non-integer weight is truncated toward zero
+ * (io_utils.c:387-395); exact_degrees = 0 reproduces that, 1 sums in double.
+ * out->a holds the Laplacian's values on A's pattern. */
+int gb_mm_read_laplacian(const char *path, int weighted, int exact_degrees, gb_mm_csr *out);
+int gb_mm_parse_laplacian(const char *bytes, long long len, int weighted, int exact_degrees,
+                          gb_mm_csr *out);
+/* The driver's right-hand side (cg_driver.c:159-230): b_i = (-1)^i, minus
+ * its component along the null vector e/sqrt(n) (weighted = 0) or
+ * sqrt(d)/||sqrt(d)|| (weighted = 1, d the Laplacian's diagonal, read from
+ * ia/ja/a), with LAP's BLAS-1 call sequence on the legacy default stream.
+ * b: device [n] (output); work: device scratch [n]. */
+int gb_laplacian_rhs(int n, const int *ia, const int *ja, const double *a, int weighted, double *b,
+                     double *work);
+
 #ifdef __cplusplus
 }
 #endif

@@ -106,6 +106,9 @@ def _proto(L: C.CDLL) -> None:
         "gb_mm_read_csr": (i, [C.c_char_p, C.POINTER(MmCsr)]),
         "gb_mm_parse_csr": (i, [C.c_char_p, C.c_longlong, C.POINTER(MmCsr)]),
         "gb_mm_csr_free": (i, [C.POINTER(MmCsr)]),
+        "gb_mm_read_laplacian": (i, [C.c_char_p, i, i, C.POINTER(MmCsr)]),
+        "gb_mm_parse_laplacian": (i, [C.c_char_p, C.c_longlong, i, i, C.POINTER(MmCsr)]),
+        "gb_laplacian_rhs": (i, [i, vp, vp, vp, i, vp, vp]),
         "gb_profile_iteration": (i, [vp, vp, vp, i, i, C.c_char_p, i, vp, vp, i, C.POINTER(i)]),
         # LAP surface
         "cuda_dot": (d, [i, vp, vp]),
@@ -372,14 +375,23 @@ class Batch:
             pass
 
 
-def read_mm_device(path=None, data: bytes | None = None):
+def read_mm_device(path=None, data: bytes | None = None, laplacian: dict | None = None):
     """A Matrix Market coordinate file (``path``, or its bytes ``data``) parsed
-    into CSR on the device (gb_mm_read_csr / gb_mm_parse_csr).  Returns
-    (ia, ja, a) as CUDA tensors and an info dict (sizes, flags, timings)."""
+    into CSR on the device (gb_mm_read_csr / gb_mm_parse_csr).  With
+    ``laplacian=dict(weighted=0|1, exact_degrees=0|1)`` the file is an
+    adjacency matrix turned into its graph Laplacian (gb_mm_read_laplacian).
+    Returns (ia, ja, a) as CUDA tensors and an info dict (sizes, flags,
+    timings)."""
     import torch
 
     out = MmCsr()
-    if data is not None:
+    if laplacian is not None:
+        w, ex = int(laplacian.get("weighted", 0)), int(laplacian.get("exact_degrees", 0))
+        if data is not None:
+            rc = lib().gb_mm_parse_laplacian(data, len(data), w, ex, C.byref(out))
+        else:
+            rc = lib().gb_mm_read_laplacian(os.fsencode(path), w, ex, C.byref(out))
+    elif data is not None:
         rc = lib().gb_mm_parse_csr(data, len(data), C.byref(out))
     else:
         rc = lib().gb_mm_read_csr(os.fsencode(path), C.byref(out))
@@ -398,6 +410,19 @@ def read_mm_device(path=None, data: bytes | None = None):
     info = {k: getattr(out, k) for k in ("n", "m", "nnz_file", "nnz", "symmetric", "pattern", "host_parsed",
                                          "read_ms", "h2d_ms", "device_ms")}
     return ia, ja, a, info
+
+
+def laplacian_rhs(ia, ja, a, weighted=0):
+    """The Laplacian driver's projected right-hand side (gb_laplacian_rhs)."""
+    import torch
+
+    n = ia.numel() - 1
+    b = torch.empty(n, dtype=torch.float64, device="cuda")
+    work = torch.empty(n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    check(lib().gb_laplacian_rhs(n, ptr(ia), ptr(ja), ptr(a), int(weighted), ptr(b), ptr(work)),
+          "gb_laplacian_rhs")
+    return b
 
 
 def _copy_dev(dst, src_ptr, count, size):

@@ -421,6 +421,19 @@ __global__ void __launch_bounds__(kMmThreads)
   }
 }
 
+// Adjacency files (read_adjacency_file, io_utils.c:128-135): after the file's
+// entries, one unit diagonal entry per vertex, entry index nnz + j.
+__global__ void diag_keys_kernel(int n, long long nnz, int cb, u64* keys, double* vals, int* ndiag) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const long long e = nnz + j;
+  keys[2 * e] = (u64)j << cb | (u64)j;
+  vals[2 * e] = 1.0;
+  keys[2 * e + 1] = (u64)n << cb;
+  vals[2 * e + 1] = 0.0;
+  atomicAdd(ndiag, 1);
+}
+
 // ------------------------------------------------------------ radix sort
 // Stable LSD radix sort of (key, value) pairs, 8-bit digits.  A block takes
 // a tile of 16 items per thread; warp w owns items [w * 512, (w + 1) * 512)
@@ -512,7 +525,50 @@ __global__ void cols_vals_kernel(const u64* __restrict__ keys, const double* __r
   }
 }
 
+// ------------------------------------------------------------ Laplacian
+// create_L_and_split (io_utils.c:367-491) on A's CSR in place.  Degrees:
+// DD[i] = -1 plus the row's values, summed left to right into an int, so
+// every partial sum is truncated toward zero (io_utils.c:387-395); exact = 1
+// sums in double instead.  One thread per row keeps that order.
+__global__ void lap_degree_kernel(int n, const int* __restrict__ ia, const double* __restrict__ a, int exact,
+                                  double* deg) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (exact) {
+    double d = -1.0;
+    for (int k = ia[i]; k < ia[i + 1]; ++k) d += a[k];
+    deg[i] = d;
+  } else {
+    int d = -1;
+    for (int k = ia[i]; k < ia[i + 1]; ++k) d = (int)((double)d + a[k]);
+    deg[i] = (double)d;
+  }
+}
+
+// unweighted: diagonal = degree, off-diagonal = -w; weighted: diagonal 1,
+// off-diagonal ((-1 * w) * (1/sqrt(d_i))) * (1/sqrt(d_j)), in the
+// reference's order of operations
+__global__ void lap_values_kernel(int n, const int* __restrict__ ia, const int* __restrict__ ja, double* a,
+                                  const double* __restrict__ deg, int weighted) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double dsq = weighted ? 1.0 / sqrt(deg[i]) : 0.0;
+  for (int k = ia[i]; k < ia[i + 1]; ++k) {
+    const int c = ja[k];
+    if (c == i) a[k] = weighted ? 1.0 : deg[i];
+    else if (!weighted) a[k] = (-1.0) * a[k];
+    else a[k] = __dmul_rn(__dmul_rn((-1.0) * a[k], dsq), 1.0 / sqrt(deg[c]));
+  }
+}
+
 // ------------------------------------------------------------ host
+// What to build from the file.
+struct MmMode {
+  bool adjacency = false;  // read_adjacency_file: symmetric, unit diagonal placeholders
+  bool laplacian = false;  // then create_L_and_split's in-place Laplacian
+  int weighted = 0, exact = 0;
+};
+
 struct Header {
   bool pattern = false, symmetric = false;
   long long n = 0, m = 0, nnz = 0;
@@ -577,12 +633,13 @@ int bits_for(long long v) {  // bits to hold 0..v
 }
 
 // The conversion from host bytes (the whole file).
-int mm_csr_from_bytes(const char* hb, long long len, gb_mm_csr* out, double read_ms) {
+int mm_csr_from_bytes(const char* hb, long long len, gb_mm_csr* out, double read_ms, const MmMode& mode) {
   Header h;
   if (!parse_header(hb, len, &h)) {
     fprintf(stderr, "libgblap: Matrix Market: no size line\n");
     return GB_BAD_INPUT;
   }
+  if (mode.adjacency) h.symmetric = true;  // io_utils.c:96
   if (h.n <= 0 || h.m <= 0 || h.nnz < 0 || h.n >= (1LL << 31) - 1 || h.m >= (1LL << 31) - 1 ||
       (h.symmetric ? 2 : 1) * h.nnz >= (1LL << 31) - 1)
     return h.n <= 0 || h.m <= 0 || h.nnz < 0 ? GB_BAD_INPUT : GB_NOT_SUPPORTED;
@@ -679,7 +736,9 @@ int mm_csr_from_bytes(const char* hb, long long len, gb_mm_csr* out, double read
     GB_CUDA_TRY(cudaStreamSynchronize(s));
   }
   // 4. keys in file order, then the sort
-  const long long slots = (h.symmetric ? 2 : 1) * h.nnz;
+  const long long entries = h.nnz + (mode.adjacency ? h.n : 0);
+  if ((h.symmetric ? 2 : 1) * entries >= (1LL << 31) - 1) return GB_NOT_SUPPORTED;
+  const long long slots = (h.symmetric ? 2 : 1) * entries;
   const int cb = bits_for(std::max(m - 1, 1));
   const int rb = bits_for(n);  // row n is the sentinel
   u64 *k0 = nullptr, *k1 = nullptr;
@@ -690,6 +749,7 @@ int mm_csr_from_bytes(const char* hb, long long len, gb_mm_csr* out, double read
   GB_TRY(D.get(&v1, slots));
   make_keys_kernel<<<ceil_div(L, kMmThreads), kMmThreads, 0, s>>>(L, flag, rank, row, col, val, h.nnz,
                                                                    h.symmetric ? 1 : 0, cb, n, k0, v0, ctl + 4);
+  if (mode.adjacency) diag_keys_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, h.nnz, cb, k0, v0, ctl + 4);
   GB_CUDA_TRY(cudaGetLastError());
   if (slots > 0) {
     const int nblk = (int)((slots + kRsTile - 1) / kRsTile);
@@ -724,6 +784,12 @@ int mm_csr_from_bytes(const char* hb, long long len, gb_mm_csr* out, double read
   row_ptr_kernel<<<ceil_div(n + 1, 256), 256, 0, s>>>(k0, nk, n, cb, ia);
   cols_vals_kernel<<<std::max(1, std::min(ceil_div((int)std::min<long long>(nk, 1 << 30), 256), 8 * device_sm_count())),
                      256, 0, s>>>(k0, v0, nk, (1ULL << cb) - 1, ja, a);
+  if (mode.laplacian) {
+    double* deg = nullptr;
+    GB_TRY(D.get(&deg, n));
+    lap_degree_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, ia, a, mode.exact, deg);
+    lap_values_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, ia, ja, a, deg, mode.weighted);
+  }
   GB_CUDA_TRY(cudaEventRecord(ev[2], s));
   const cudaError_t e = cudaStreamSynchronize(s);
   if (e != cudaSuccess || cudaGetLastError() != cudaSuccess) {
@@ -757,10 +823,12 @@ int mm_csr_from_bytes(const char* hb, long long len, gb_mm_csr* out, double read
 extern "C" int gb_mm_parse_csr(const char* bytes, long long len, gb_mm_csr* out) {
   if (!bytes || len <= 0 || !out) return GB_BAD_INPUT;
   memset(out, 0, sizeof *out);
-  return gb::mm_csr_from_bytes(bytes, len, out, 0.0);
+  return gb::mm_csr_from_bytes(bytes, len, out, 0.0, gb::MmMode());
 }
 
-extern "C" int gb_mm_read_csr(const char* path, gb_mm_csr* out) {
+namespace gb {
+namespace {
+int mm_read_file(const char* path, gb_mm_csr* out, const MmMode& mode) {
   if (!path || !out) return GB_BAD_INPUT;
   memset(out, 0, sizeof *out);
   const auto t0 = std::chrono::steady_clock::now();
@@ -786,9 +854,32 @@ extern "C" int gb_mm_read_csr(const char* path, gb_mm_csr* out) {
   fclose(f);
   const double read_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   int rc = GB_BAD_INPUT;
-  if ((long long)got == len) rc = gb::mm_csr_from_bytes(hb, len, out, read_ms);
+  if ((long long)got == len) rc = mm_csr_from_bytes(hb, len, out, read_ms, mode);
   cudaFreeHost(hb);
   return rc;
+}
+
+MmMode laplacian_mode(int weighted, int exact) {
+  MmMode m;
+  m.adjacency = m.laplacian = true;
+  m.weighted = weighted ? 1 : 0;
+  m.exact = exact ? 1 : 0;
+  return m;
+}
+}  // namespace
+}  // namespace gb
+
+extern "C" int gb_mm_read_csr(const char* path, gb_mm_csr* out) { return gb::mm_read_file(path, out, gb::MmMode()); }
+
+extern "C" int gb_mm_read_laplacian(const char* path, int weighted, int exact_degrees, gb_mm_csr* out) {
+  return gb::mm_read_file(path, out, gb::laplacian_mode(weighted, exact_degrees));
+}
+
+extern "C" int gb_mm_parse_laplacian(const char* bytes, long long len, int weighted, int exact_degrees,
+                                     gb_mm_csr* out) {
+  if (!bytes || len <= 0 || !out) return GB_BAD_INPUT;
+  memset(out, 0, sizeof *out);
+  return gb::mm_csr_from_bytes(bytes, len, out, 0.0, gb::laplacian_mode(weighted, exact_degrees));
 }
 
 extern "C" int gb_mm_csr_free(gb_mm_csr* m) {
@@ -798,5 +889,63 @@ extern "C" int gb_mm_csr_free(gb_mm_csr* m) {
   cudaFree(m->a);
   m->ia = m->ja = nullptr;
   m->a = nullptr;
+  return GB_OK;
+}
+
+// ------------------------------------------------------------ projected right-hand side
+// cg_driver.c:159-230: b_i = (-1)^i, then b minus its component along the
+// Laplacian's null vector -- e / sqrt(n) (unweighted), or sqrt(d) e /
+// ||sqrt(d) e|| (weighted, d the diagonal) -- with the same BLAS-1 calls in
+// the same order (scal, dot, axpy; vector_sqrt, vec_vec), on the legacy
+// default stream as LAP's backend runs them.
+extern "C" double cuda_dot(const int n, const double* v, const double* w);
+extern "C" void cuda_scal(const int n, const double alpha, double* v);
+extern "C" void cuda_axpy(const int n, const double alpha, const double* x, double* y);
+extern "C" void cuda_vec_vec(const int n, const double* x, const double* y, double* res);
+extern "C" void cuda_vector_sqrt(const int n, const double* v, double* res);
+
+namespace gb {
+namespace {
+__global__ void rhs_init_kernel(int n, double* b, double* e) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  b[i] = (i % 2) ? -1.0 : 1.0;  // pow(-1.0, i % 2)
+  e[i] = 1.0;
+}
+__global__ void diagonal_kernel(int n, const int* __restrict__ ia, const int* __restrict__ ja,
+                                const double* __restrict__ a, double* d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double v = 0.0;
+  for (int k = ia[i]; k < ia[i + 1]; ++k)
+    if (ja[k] == i) v = a[k];
+  d[i] = v;
+}
+}  // namespace
+}  // namespace gb
+
+extern "C" int gb_laplacian_rhs(int n, const int* ia, const int* ja, const double* a, int weighted, double* b,
+                                double* work) {
+  if (n <= 0 || !b || !work || (weighted && (!ia || !ja || !a))) return GB_BAD_INPUT;
+  double* e = work;  // [n]
+  gb::rhs_init_kernel<<<gb::ceil_div(n, 256), 256>>>(n, b, e);
+  GB_CUDA_TRY(cudaGetLastError());
+  if (!weighted) {
+    const double one_over_norme = 1. / sqrt((double)n);
+    cuda_scal(n, one_over_norme, e);
+    const double be = -cuda_dot(n, e, b);
+    cuda_axpy(n, be, e, b);
+  } else {
+    double* aux = work;  // d, then sqrt(d); vec_vec(aux, e) with e = 1 leaves it unchanged
+    gb::diagonal_kernel<<<gb::ceil_div(n, 256), 256>>>(n, ia, ja, a, aux);
+    GB_CUDA_TRY(cudaGetLastError());
+    cuda_vector_sqrt(n, aux, aux);
+    double de_norm = cuda_dot(n, aux, aux);
+    de_norm = 1.0 / sqrt(de_norm);
+    cuda_scal(n, de_norm, aux);
+    const double bwe = -cuda_dot(n, b, aux);
+    cuda_axpy(n, bwe, aux, b);
+  }
+  GB_CUDA_TRY(cudaDeviceSynchronize());
   return GB_OK;
 }

@@ -213,7 +213,7 @@ def _strtod_prefix(tok: str) -> float:
     return float(m.group(0))
 
 
-def mm_csr(data: bytes):
+def mm_csr(data: bytes, adjacency: bool = False):
     """read_mm_file (io_utils.c:15-74) + coo_to_csr (io_utils.c:141-235) on
     the bytes of a Matrix Market coordinate file, restated in Python/numpy.
 
@@ -224,12 +224,15 @@ def mm_csr(data: bytes):
     mirrored (:150-157, :177-194); rows bucketed in encounter order, then each
     row sorted by column with equal columns kept in that order (:199-210, the
     reference's qsort being glibc's merge sort here).
+    adjacency=True follows read_adjacency_file (io_utils.c:82-138) instead:
+    symmetric whatever the banner says, and one unit diagonal entry per
+    vertex after the file's entries.
     Returns (n, m, symmetric, ia, ja, a)."""
     text = data.decode("ascii", errors="replace")
     lines = text.split("\n")
     banner = lines[0]
     pattern = "pattern" in banner
-    symmetric = "symmetric" in banner
+    symmetric = "symmetric" in banner or adjacency
     k = 1
     while k < len(lines) and lines[k].startswith("%"):
         k += 1
@@ -250,6 +253,10 @@ def mm_csr(data: bytes):
         vals.append(1.0 if pattern else _strtod_prefix(parts[2]))
     if len(rows) < nnz:
         raise ValueError(f"file ended after {len(rows)} of {nnz} entries")
+    if adjacency:
+        rows += list(range(n))
+        cols += list(range(n))
+        vals += [1.0] * n
     r = np.array(rows, dtype=np.int64)
     c = np.array(cols, dtype=np.int64)
     v = np.array(vals, dtype=np.float64)
@@ -269,3 +276,51 @@ def mm_csr(data: bytes):
     ia = np.zeros(n + 1, dtype=np.int32)
     np.cumsum(np.bincount(r, minlength=n), out=ia[1:])
     return n, m, symmetric, ia, c.astype(np.int32), v
+
+
+def laplacian_csr(data: bytes, weighted: int = 0, exact_degrees: int = 0):
+    """The Laplacian driver's matrix (cg_driver.c:38-45): read_adjacency_file
+    + coo_to_csr (mm_csr(adjacency=True)), then create_L_and_split's
+    in-place Laplacian (io_utils.c:367-491).  Degrees are summed into an int
+    as the reference does, every partial sum truncated toward zero
+    (io_utils.c:387-395), unless exact_degrees.  Returns (n, ia, ja, a)."""
+    import math
+
+    n, _, _, ia, ja, a = mm_csr(data, adjacency=True)
+    a = a.copy()
+    deg = np.zeros(n)
+    for i in range(n):
+        if exact_degrees:
+            d = -1.0
+            for k in range(ia[i], ia[i + 1]):
+                d += a[k]
+        else:
+            d = -1
+            for k in range(ia[i], ia[i + 1]):
+                d = int(d + a[k])  # C: int += double truncates toward zero
+        deg[i] = d
+    out = a.copy()
+    for i in range(n):
+        dsq = 1.0 / math.sqrt(deg[i]) if weighted else 0.0
+        for k in range(ia[i], ia[i + 1]):
+            c = ja[k]
+            if c == i:
+                out[k] = 1.0 if weighted else deg[i]
+            elif not weighted:
+                out[k] = -1.0 * a[k]
+            else:
+                out[k] = (-1.0) * a[k] * dsq * (1.0 / math.sqrt(deg[c]))
+    return n, ia, ja, out
+
+
+def laplacian_rhs(n, diag, weighted=0):
+    """cg_driver.c:159-230: b_i = (-1)^i minus its component along e/sqrt(n)
+    (unweighted) or sqrt(d)/||sqrt(d)|| (weighted); numpy sums, so the last
+    bits may differ from a device dot."""
+    b = np.where(np.arange(n) % 2, -1.0, 1.0)
+    if not weighted:
+        e = np.ones(n) * (1.0 / np.sqrt(n))
+    else:
+        e = np.sqrt(np.asarray(diag, dtype=np.float64))
+        e = e * (1.0 / np.sqrt(np.dot(e, e)))
+    return b - np.dot(e, b) * e

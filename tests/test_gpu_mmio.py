@@ -100,3 +100,66 @@ def test_edge_cases():
 def test_rejects_bad_files(text):
     with pytest.raises(gb.GbError):
         gb.read_mm_device(data=text.encode())
+
+
+def _adjacency_bytes(weights, seed=5, n=300, m=1500):
+    rng = np.random.default_rng(seed)
+    ei, ej = rng.integers(0, n, m), rng.integers(0, n, m)
+    keep = ei != ej
+    ei, ej = ei[keep], ej[keep]
+    lo, hi = np.maximum(ei, ej) + 1, np.minimum(ei, ej) + 1
+    kind = "real" if weights else "pattern"
+    lines = [f"%%MatrixMarket matrix coordinate {kind} symmetric", f"{n} {n} {lo.shape[0]}"]
+    if weights:
+        w = rng.uniform(0.1, 3.0, lo.shape[0])
+        lines += [f"{lo[i]} {hi[i]} {w[i]!r}" for i in range(lo.shape[0])]
+    else:
+        lines += [f"{lo[i]} {hi[i]}" for i in range(lo.shape[0])]
+    return ("\n".join(lines) + "\n").encode()
+
+
+@pytest.mark.parametrize("weights", [False, True])
+@pytest.mark.parametrize("weighted", [0, 1])
+@pytest.mark.parametrize("exact", [0, 1])
+def test_laplacian_from_adjacency(weights, weighted, exact):
+    """gb_mm_parse_laplacian against oracle.laplacian_csr (pinned to the
+    reference's builder): int-truncated degrees by default, exact ones with
+    the flag -- the two differ once weights are not integers."""
+    data = _adjacency_bytes(weights)
+    ia, ja, a, info = gb.read_mm_device(data=data, laplacian=dict(weighted=weighted, exact_degrees=exact))
+    n, oia, oja, oa = oracle.laplacian_csr(data, weighted, exact)
+    assert info["symmetric"] == 1 and info["n"] == n
+    assert np.array_equal(ia.cpu().numpy(), oia) and np.array_equal(ja.cpu().numpy(), oja)
+    assert np.array_equal(a.cpu().numpy().view(np.int64), oa.view(np.int64))
+    if weights and not weighted:
+        _, _, _, trunc = oracle.laplacian_csr(data, 0, 0)
+        _, _, _, full = oracle.laplacian_csr(data, 0, 1)
+        assert not np.array_equal(trunc, full)  # the flag matters here
+
+
+def test_laplacian_reference_fixture(golden):
+    ia, ja, a, _ = gb.read_mm_device(f"{ROOT}/tests/golden/adj5.mtx", laplacian=dict(weighted=0))
+    assert np.array_equal(ia.cpu().numpy(), golden["adj_ia"]) and np.array_equal(ja.cpu().numpy(), golden["adj_ja"])
+    assert np.array_equal(a.cpu().numpy(), golden["adj_a"])
+
+
+@pytest.mark.parametrize("weighted", [0, 1])
+def test_laplacian_rhs_and_solve(weighted):
+    """The driver's projected right-hand side is orthogonal to the null
+    vector and matches the oracle's to rounding; the singular Laplacian
+    system then solves (cg_driver.c's flow, on the device)."""
+    data = _adjacency_bytes(False, n=400, m=4000)
+    ia, ja, a, _ = gb.read_mm_device(data=data, laplacian=dict(weighted=weighted))
+    b = gb.laplacian_rhs(ia, ja, a, weighted)
+    n = ia.numel() - 1
+    A = gen.CSR(n, ia.cpu().numpy(), ja.cpu().numpy(), a.cpu().numpy())
+    rows = np.repeat(np.arange(n), np.diff(A.ia))
+    diag = A.a[A.ja == rows]
+    ref = oracle.laplacian_rhs(n, diag, weighted)
+    assert np.abs(b.cpu().numpy() - ref).max() <= 1e-14 * np.abs(ref).max() + 1e-15
+    null = np.sqrt(diag) if weighted else np.ones(n)
+    assert abs(float(np.dot(b.cpu().numpy(), null))) < 1e-10 * np.linalg.norm(null)
+    sysm = gb.System.from_csr(A, "line_jacobi")
+    x, r = sysm.solve(b, tol=1e-8, maxit=5000)
+    assert r["flag"] == 0
+    sysm.close()

@@ -150,3 +150,46 @@ def test_mm_csr_oracle_matches_reference_reader(kind, tmp_path):
     _, _, _, oia, oja, oa = oracle.mm_csr(text.encode())
     assert np.array_equal(ia, oia) and np.array_equal(ja, oja)
     assert np.array_equal(a.view(np.int64), oa.view(np.int64))
+
+
+def test_laplacian_oracle_matches_reference_fixture(golden):
+    with open(os.path.join(ROOT, "tests", "golden", "adj5.mtx"), "rb") as f:
+        n, ia, ja, a = oracle.laplacian_csr(f.read(), weighted=0)
+    assert np.array_equal(ia, golden["adj_ia"]) and np.array_equal(ja, golden["adj_ja"])
+    assert np.array_equal(a, golden["adj_a"])
+
+
+def _random_adjacency(tmp_path, weights, seed=5, n=200, m=800):
+    rng = np.random.default_rng(seed)
+    ei, ej = rng.integers(0, n, m), rng.integers(0, n, m)
+    keep = ei != ej
+    ei, ej = ei[keep], ej[keep]
+    w = rng.uniform(0.1, 3.0, ei.shape[0]) if weights else None
+    p = tmp_path / f"adj_{int(weights)}.mtx"
+    gen.write_adjacency(str(p), n, ei, ej, w)
+    return p
+
+
+@pytest.mark.parametrize("weights", [False, True])
+@pytest.mark.parametrize("weighted", [0, 1])
+def test_laplacian_oracle_matches_reference_builder(tmp_path, weights, weighted):
+    """oracle.laplacian_csr against the reference's read_adjacency_file +
+    coo_to_csr + create_L_and_split on random graphs with repeated edges;
+    non-integer weights exercise its int degree truncation."""
+    L = oracle.ref_lib()
+    if L is None:
+        pytest.skip("reference library not built here")
+    p = _random_adjacency(tmp_path, weights)
+    L.ref_read_laplacian_csr.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                         C.POINTER(C.POINTER(C.c_int)), C.POINTER(C.POINTER(C.c_int)),
+                                         C.POINTER(C.POINTER(C.c_double))]
+    n, nnz = C.c_int(), C.c_int()
+    pia, pja, pa = C.POINTER(C.c_int)(), C.POINTER(C.c_int)(), C.POINTER(C.c_double)()
+    L.ref_read_laplacian_csr(str(p).encode(), weighted, C.byref(n), C.byref(nnz), C.byref(pia), C.byref(pja),
+                             C.byref(pa))
+    ia = np.ctypeslib.as_array(pia, (n.value + 1,)).copy()
+    ja = np.ctypeslib.as_array(pja, (nnz.value,)).copy()
+    a = np.ctypeslib.as_array(pa, (nnz.value,)).copy()
+    _, oia, oja, oa = oracle.laplacian_csr(p.read_bytes(), weighted)
+    assert np.array_equal(ia, oia) and np.array_equal(ja, oja)
+    assert np.array_equal(a.view(np.int64), oa.view(np.int64))
