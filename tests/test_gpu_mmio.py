@@ -112,7 +112,7 @@ def _adjacency_bytes(weights, seed=5, n=300, m=1500):
     lines = [f"%%MatrixMarket matrix coordinate {kind} symmetric", f"{n} {n} {lo.shape[0]}"]
     if weights:
         w = rng.uniform(0.1, 3.0, lo.shape[0])
-        lines += [f"{lo[i]} {hi[i]} {w[i]!r}" for i in range(lo.shape[0])]
+        lines += [f"{lo[i]} {hi[i]} {float(w[i])!r}" for i in range(lo.shape[0])]
     else:
         lines += [f"{lo[i]} {hi[i]}" for i in range(lo.shape[0])]
     return ("\n".join(lines) + "\n").encode()
