@@ -300,16 +300,18 @@ def laplacian_csr(data: bytes, weighted: int = 0, exact_degrees: int = 0):
                 d = int(d + a[k])  # C: int += double truncates toward zero
         deg[i] = d
     out = a.copy()
-    for i in range(n):
-        dsq = 1.0 / math.sqrt(deg[i]) if weighted else 0.0
-        for k in range(ia[i], ia[i + 1]):
-            c = ja[k]
-            if c == i:
-                out[k] = 1.0 if weighted else deg[i]
-            elif not weighted:
-                out[k] = -1.0 * a[k]
-            else:
-                out[k] = (-1.0) * a[k] * dsq * (1.0 / math.sqrt(deg[c]))
+    one = np.float64(1.0)
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):  # IEEE results, as C gives
+        for i in range(n):
+            dsq = one / np.sqrt(np.float64(deg[i])) if weighted else 0.0
+            for k in range(ia[i], ia[i + 1]):
+                c = ja[k]
+                if c == i:
+                    out[k] = 1.0 if weighted else deg[i]
+                elif not weighted:
+                    out[k] = -1.0 * a[k]
+                else:
+                    out[k] = (np.float64(-1.0) * a[k]) * dsq * (one / np.sqrt(np.float64(deg[c])))
     return n, ia, ja, out
 
 
