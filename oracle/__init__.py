@@ -284,8 +284,6 @@ def laplacian_csr(data: bytes, weighted: int = 0, exact_degrees: int = 0):
     in-place Laplacian (io_utils.c:367-491).  Degrees are summed into an int
     as the reference does, every partial sum truncated toward zero
     (io_utils.c:387-395), unless exact_degrees.  Returns (n, ia, ja, a)."""
-    import math
-
     n, _, _, ia, ja, a = mm_csr(data, adjacency=True)
     a = a.copy()
     deg = np.zeros(n)

@@ -102,12 +102,17 @@ def test_rejects_bad_files(text):
         gb.read_mm_device(data=text.encode())
 
 
-def _adjacency_bytes(weights, seed=5, n=300, m=1500):
+def _adjacency_bytes(weights, seed=5, n=300, m=1500, unique=False):
+    """A random graph's adjacency, lower triangle; repeated edges unless
+    unique (the solver takes no duplicate entries)."""
     rng = np.random.default_rng(seed)
     ei, ej = rng.integers(0, n, m), rng.integers(0, n, m)
     keep = ei != ej
     ei, ej = ei[keep], ej[keep]
     lo, hi = np.maximum(ei, ej) + 1, np.minimum(ei, ej) + 1
+    if unique:
+        pairs = np.unique(np.stack([lo, hi], 1), axis=0)
+        lo, hi = pairs[:, 0], pairs[:, 1]
     kind = "real" if weights else "pattern"
     lines = [f"%%MatrixMarket matrix coordinate {kind} symmetric", f"{n} {n} {lo.shape[0]}"]
     if weights:
@@ -151,7 +156,7 @@ def test_laplacian_rhs_and_solve(weighted):
     device).  The weighted driver projects out sqrt(diag) = e as well, while
     I - D^-1/2 W D^-1/2 has null vector D^1/2 e, so that system is left
     unsolved here, as the reference leaves it inconsistent."""
-    data = _adjacency_bytes(False, n=400, m=4000)
+    data = _adjacency_bytes(False, n=400, m=4000, unique=True)
     ia, ja, a, _ = gb.read_mm_device(data=data, laplacian=dict(weighted=weighted))
     b = gb.laplacian_rhs(ia, ja, a, weighted)
     n = ia.numel() - 1
