@@ -45,6 +45,8 @@ const char *gb_status_str(int status);
 int gb_prec_from_name(const char *name);
 /* Library build string (arch, version). */
 const char *gb_version(void);
+/* Waits for all device work the calling thread has queued (cudaDeviceSynchronize). */
+int gb_synchronize(void);
 
 /* ------------------------------------------------------------ solver object */
 typedef struct gb_system_s *gb_system;

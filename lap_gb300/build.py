@@ -64,9 +64,28 @@ def build(jobs: int | None = None, debug: bool = False, quiet: bool = True) -> s
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    _build_driver(LIB)
     if not quiet:
         print("built", LIB)
     return LIB
+
+
+DRIVER_SRC = os.path.join(CSRC, "lap_mm_driver.c")
+DRIVER = os.path.join(HERE, "lap_mm_driver")
+
+
+def _build_driver(lib: str) -> None:
+    """LAP's SpMV benchmark program (mm_driver.c) on the library: a plain C
+    host program linked against libgblap.so (found next to it at run time)."""
+    if os.path.exists(DRIVER) and os.path.getmtime(DRIVER) >= max(os.path.getmtime(lib),
+                                                                   os.path.getmtime(DRIVER_SRC)):
+        return
+    cc = shutil.which("gcc") or shutil.which("cc")
+    cmd = [cc, "-O2", "-std=c11", "-I" + os.path.join(ROOT, "include"), DRIVER_SRC, "-L" + HERE, "-lgblap",
+           "-Wl,-rpath,$ORIGIN", "-lm", "-o", DRIVER]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
 
 
 if __name__ == "__main__":

@@ -949,3 +949,8 @@ extern "C" int gb_laplacian_rhs(int n, const int* ia, const int* ja, const doubl
   GB_CUDA_TRY(cudaDeviceSynchronize());
   return GB_OK;
 }
+
+extern "C" int gb_synchronize(void) {
+  GB_CUDA_TRY(cudaDeviceSynchronize());
+  return GB_OK;
+}

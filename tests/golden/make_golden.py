@@ -135,6 +135,15 @@ def main() -> None:
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", len(out), "arrays")
 
+    # the reference's SpMV benchmark program (mm_driver.c) on grid6.mtx, 3 trials:
+    # its report, against which the library's lap_mm_driver is compared
+    import subprocess
+
+    drv = os.path.join(ROOT, "oracle", "_ref", "mm_driver")
+    rep = subprocess.run([drv, mm, "3"], capture_output=True, text=True, check=True).stdout
+    with open(os.path.join(HERE, "mm_driver_grid6.txt"), "w") as f:
+        f.write(rep)
+
 
 if __name__ == "__main__":
     main()

@@ -172,3 +172,31 @@ def test_laplacian_rhs_and_solve(weighted):
         x, r = sysm.solve(b, tol=1e-8, maxit=5000)
         assert r["flag"] == 0
         sysm.close()
+
+
+def test_spmv_driver_report_matches_reference():
+    """lap_mm_driver (mm_driver.c on the library) prints the reference
+    program's report line for line: tests/golden/mm_driver_grid6.txt is the
+    reference's own output on grid6.mtx with 3 trials.  The two time lines
+    carry this run's times, and ||A x|| may differ from the reference's serial
+    dot in the last bits."""
+    import os
+    import re
+    import subprocess
+
+    drv = os.path.join(ROOT, "lap_gb300", "lap_mm_driver")
+    out = subprocess.run([drv, f"{ROOT}/tests/golden/grid6.mtx", "3"], capture_output=True, text=True,
+                         check=True).stdout.split("\n")
+    ref = open(f"{ROOT}/tests/golden/mm_driver_grid6.txt").read().split("\n")
+    assert len(out) == len(ref)
+    for got, want in zip(out, ref):
+        if "Time (" in want:
+            pat = re.escape(want[: want.index(":") + 2]) + r"\d+\.\d{16}  $"
+            assert re.match(pat, got), (got, want)
+        elif "Norm of A*x" in want:
+            head = want[: want.index(":") + 2]
+            assert got.startswith(head) and re.match(re.escape(head) + r"-?\d\.\d{16}e[+-]\d\d  $", got)
+            g, w = float(got[len(head):]), float(want[len(head):])
+            assert abs(g - w) <= 1e-14 * abs(w)
+        else:
+            assert got == want
