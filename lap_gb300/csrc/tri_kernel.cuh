@@ -606,17 +606,21 @@ __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArg
 }
 
 int tri_blocks_per_sm();
-// CTAs per cluster for FP32 solves: -1 automatic (8 or 4), 0 per-CTA form,
-// 4 or 8 forced (GBLAP_TRI_CLUSTER)
+// CTAs per cluster for FP32 solves: -1 automatic (16, 8 or 4), 0 per-CTA
+// form, 4, 8 or 16 forced (GBLAP_TRI_CLUSTER)
 int tri_cluster_size();
 
-// GB_NOT_SUPPORTED when the device cannot place one cluster of CL CTAs.
+// GB_NOT_SUPPORTED when the device cannot place one cluster of CL CTAs, or,
+// with all_resident, cannot place every group's cluster at once.
 template <typename T, typename OP, bool EXACT, int CL>
-int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, size_t smem) {
+int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, size_t smem,
+                  bool all_resident = false) {
   auto kern = tri_tile_kernel<T, OP, EXACT, CL>;
   static bool attr_set = false;  // one per instantiation
   if (!attr_set) {
     GB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kTriMaxDynSmem));
+    // clusters of more than 8 CTAs are an opt-in size
+    if (CL > 8) GB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     attr_set = true;
   }
   if constexpr (CL > 1) {
@@ -634,7 +638,8 @@ int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, 
     const int groups = (p.ntiles + CL - 1) / CL;
     cfg.gridDim = dim3(groups * CL);
     int active = 0;
-    if (cudaOccupancyMaxActiveClusters(&active, kern, &cfg) != cudaSuccess || active < 1) {
+    if (cudaOccupancyMaxActiveClusters(&active, kern, &cfg) != cudaSuccess || active < 1 ||
+        (all_resident && active < groups)) {
       cudaGetLastError();
       return GB_NOT_SUPPORTED;
     }
@@ -659,13 +664,14 @@ int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, 
 
 // Launches the tiled solve: dynamic shared memory = the record ring plus one
 // tile of T values (plus the inbox tile in the cluster form).  FP32 tiles
-// that fit with an inbox run in clusters of 8 CTAs (4 where 8 cannot be
-// placed).  On 128^3 (128 tiles) only 15 clusters of 8 fit at once, so the
-// last group starts late, and still 8 beats all-resident clusters of 4 for
-// the IC(0) solves (188 vs 201 ms per PCG solve): a tile boundary inside a
-// cluster costs a shared-memory poll, one between clusters an L2 round trip.
-// Everything else runs the per-CTA form on a persistent grid of
-// min(tiles, SMs x resident CTAs).
+// that fit with an inbox run in clusters: of 16 CTAs when every group's
+// cluster can be resident at once, else of 8 (4 where 8 cannot be placed).
+// A tile boundary inside a cluster costs a shared-memory poll, one between
+// clusters an L2 round trip; and a group that is not resident starts only
+// when an earlier cluster has finished all its tiles, which puts it late on
+// the dependency chain (on 128^3, 128 tiles: 15 clusters of 8 fit, 8 of 16
+// hold them all).  Everything else runs the per-CTA form on a persistent
+// grid of min(tiles, SMs x resident CTAs).
 template <typename T, typename OP, bool EXACT>
 int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   if (p.ntiles <= 0) return GB_OK;
@@ -676,10 +682,12 @@ int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
     const int want = tri_cluster_size();
     if (p.ntiles > 1 && smem_cl <= (size_t)kTriMaxDynSmem && want != 0) {
       int rc = GB_NOT_SUPPORTED;
-      if (want == 8) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
+      if (want == 16) rc = tri_launch_cl<T, OP, EXACT, 16>(p, A, op, s, smem_cl);
+      else if (want == 8) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
       else if (want == 4) rc = tri_launch_cl<T, OP, EXACT, 4>(p, A, op, s, smem_cl);
       else {
-        rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
+        rc = p.ntiles > 8 ? tri_launch_cl<T, OP, EXACT, 16>(p, A, op, s, smem_cl, true) : GB_NOT_SUPPORTED;
+        if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
         if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 4>(p, A, op, s, smem_cl);
       }
       if (rc != GB_NOT_SUPPORTED) return rc;

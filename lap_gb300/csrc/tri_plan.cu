@@ -395,7 +395,7 @@ int tri_cluster_size() {
   if (v == -2) {
     const char* e = getenv("GBLAP_TRI_CLUSTER");
     const int x = e ? atoi(e) : -1;
-    v = (x == 0 || x == 4 || x == 8) ? x : -1;
+    v = (x == 0 || x == 4 || x == 8 || x == 16) ? x : -1;
   }
   return v;
 }

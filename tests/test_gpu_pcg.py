@@ -316,14 +316,15 @@ def test_cluster_form_matches_per_cta_form(tmp_path):
     """The FP32 solves in thread-block clusters pass boundary values through
     distributed shared memory instead of L2: the arithmetic is the same, so
     the mixed-precision solutions must be bitwise identical to the per-CTA
-    form's (GBLAP_TRI_CLUSTER=0).  The switch is read once per process."""
+    form's (GBLAP_TRI_CLUSTER=0), in clusters of 8 and of 16 alike.  The
+    switch is read once per process."""
     import os
     import subprocess
     import sys
 
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     out = {}
-    for mode in ("0", "8"):
+    for mode in ("0", "8", "16"):
         env = dict(os.environ, GBLAP_TRI_CLUSTER=mode)
         stem = str(tmp_path / f"cl{mode}")
         subprocess.run([sys.executable, "-c", _CLUSTER_CHILD, root, stem], env=env, check=True,
@@ -332,5 +333,6 @@ def test_cluster_form_matches_per_cta_form(tmp_path):
     for prec in ("ichol", "GS_std"):
         for p in (1, 2):
             a = np.load(f"{out['0']}_{prec}_{p}.npy")
-            c = np.load(f"{out['8']}_{prec}_{p}.npy")
-            assert np.array_equal(a, c), (prec, p)
+            for cl in ("8", "16"):
+                c = np.load(f"{out[cl]}_{prec}_{p}.npy")
+                assert np.array_equal(a, c), (prec, p, cl)
