@@ -664,14 +664,14 @@ int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, 
 
 // Launches the tiled solve: dynamic shared memory = the record ring plus one
 // tile of T values (plus the inbox tile in the cluster form).  FP32 tiles
-// that fit with an inbox run in clusters: of 16 CTAs when every group's
-// cluster can be resident at once, else of 8 (4 where 8 cannot be placed).
-// A tile boundary inside a cluster costs a shared-memory poll, one between
-// clusters an L2 round trip; and a group that is not resident starts only
-// when an earlier cluster has finished all its tiles, which puts it late on
-// the dependency chain (on 128^3, 128 tiles: 15 clusters of 8 fit, 8 of 16
-// hold them all).  Everything else runs the per-CTA form on a persistent
-// grid of min(tiles, SMs x resident CTAs).
+// that fit with an inbox run in clusters of 16 CTAs (8, then 4, where 16
+// cannot be placed).  A tile boundary inside a cluster costs a shared-memory
+// poll, one between clusters an L2 round trip; a group whose cluster is not
+// resident starts only when an earlier cluster has finished all its tiles.
+// On 128^3 (128 tiles, 16 of 8 or 8 of 16 groups, not all resident either
+// way) 16 gave 177 ms per IC(0) split solve against 181 ms for 8.
+// Everything else runs the per-CTA form on a persistent grid of
+// min(tiles, SMs x resident CTAs).
 template <typename T, typename OP, bool EXACT>
 int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   if (p.ntiles <= 0) return GB_OK;
@@ -686,7 +686,7 @@ int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
       else if (want == 8) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
       else if (want == 4) rc = tri_launch_cl<T, OP, EXACT, 4>(p, A, op, s, smem_cl);
       else {
-        rc = p.ntiles > 8 ? tri_launch_cl<T, OP, EXACT, 16>(p, A, op, s, smem_cl, true) : GB_NOT_SUPPORTED;
+        rc = p.ntiles > 8 ? tri_launch_cl<T, OP, EXACT, 16>(p, A, op, s, smem_cl) : GB_NOT_SUPPORTED;
         if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
         if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 4>(p, A, op, s, smem_cl);
       }
