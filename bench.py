@@ -205,8 +205,9 @@ def run_kernels_only(args, local):
     A, b = make_workload(args.size)
     sysm = gb.System.from_csr(A, "ichol")
     db = torch.from_numpy(b).cuda()
+    precs = [int(t) for t in args.profile_precisions.split(",")]
     out = {p: [(k["name"], round(k["ms"], 5)) for k in sysm.profile(db, precision=p, iters=args.profile_iters)]
-           for p in (0, 1, 2)}
+           for p in precs}
     print(json.dumps({"kernels_only": out, "n": A.n, "nnz": A.nnz}), flush=True)
 
 
@@ -543,6 +544,8 @@ def main():
                              "mmread128"],
                     help="ichol128 is the headline line; the others are the remaining configurations")
     ap.add_argument("--fd-edges", type=int, default=16)
+    ap.add_argument("--profile-precisions", default="0,1,2",
+                    help="--kernels-only: precision modes to run (comma list of 0, 1, 2)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_init(args)
