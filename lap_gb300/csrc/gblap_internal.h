@@ -78,8 +78,12 @@ struct TriPlan {
   int n = 0;
   bool lower = true;
   int nlevels = 0;           // global dependency depth (diagnostics)
-  int tile_rows = 0;
+  int tile_rows = 0;         // 0 in the levels form
   int ntiles = 0;
+  // levels form: "tiles" are consecutive runs of records in global level
+  // order with no rows of their own (every dependency is read through L2);
+  // chosen when contiguous row tiles would hold few of the dependencies
+  bool levels_form = false;
   int nlvl = 0;              // tile-local levels, summed over tiles
   int nrec = 0;
   long long ndeps = 0;       // dependencies without padding (algorithmic size)

@@ -359,7 +359,7 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
     if (lane == 0) {
       const T r = sub_rn(acc, s);
       yv = publishable(EXACT ? div_rn(r, diag[0]) : r * dinv[0]);
-      sy[row - t0] = yv;
+      if (row >= t0 && row < t1) sy[row - t0] = yv;  // the levels form has no tile rows
     }
   } else if (act) {
     // tile-local values: complete (earlier tile-levels); all loads at once
@@ -398,7 +398,7 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
       }
     }
     yv = publishable(EXACT ? div_rn(acc, dg) : acc);
-    sy[row - t0] = yv;
+    if (row >= t0 && row < t1) sy[row - t0] = yv;  // the levels form has no tile rows
   }
   __syncwarp();
   if (lane == 0) red_release_cta_add(s_done, 1);
@@ -680,7 +680,7 @@ int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   if constexpr (sizeof(T) == 4) {
     const size_t smem_cl = smem + (size_t)p.tile_rows * sizeof(T);
     const int want = tri_cluster_size();
-    if (p.ntiles > 1 && smem_cl <= (size_t)kTriMaxDynSmem && want != 0) {
+    if (p.ntiles > 1 && !p.levels_form && smem_cl <= (size_t)kTriMaxDynSmem && want != 0) {
       int rc = GB_NOT_SUPPORTED;
       if (want == 16) rc = tri_launch_cl<T, OP, EXACT, 16>(p, A, op, s, smem_cl);
       else if (want == 8) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);

@@ -2,6 +2,7 @@
 // csrsv2 analysis of cuda_blas.cu:99-224) and its launchers.
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "gb_common.cuh"
@@ -39,6 +40,8 @@ namespace {
 // single row of kLongDeps dependencies must fit a ring slot:
 // header + 4*4 + 2*8*4 + kLongDeps*4*12 <= kTriSlotBytes.
 constexpr int kLongDeps = 32;
+// levels form: records per ticket (one CTA's run of records)
+constexpr int kLevelTileRecs = 128;
 static_assert(kRecHdrBytes + 16 + 64 + kLongDeps * 4 * 12 <= kTriSlotBytes, "record slot too small");
 
 // bytes of a SHORT record with `rows` rows of up to `len` dependencies
@@ -167,12 +170,79 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
     }
   }
 
-  // tiles -> tile-local levels -> records
-  const int ntiles = (n + tile_rows - 1) / tile_rows;
+  // Form.  Contiguous row tiles keep a dependency inside the tile (shared
+  // memory) when rows and their dependencies are near in index, as on grids.
+  // When most dependencies cross tiles (a random labelling, power-law
+  // graphs) the levels form takes over: records in global level order, cut
+  // into runs of kLevelTileRecs records that CTAs take by ticket; with no
+  // rows of their own, every dependency is read through L2.  Tiled, a tile
+  // would wait on many earlier tiles, and tiles not yet resident start only
+  // when whole earlier tiles have finished.  GBLAP_TRI_FORM=tiles|levels
+  // forces a form.
+  bool levels_form = false;
+  {
+    long long cross = 0;
+    for (int i = 0; i < n; ++i)
+      for (int k = d.row_ptr[i]; k < d.row_ptr[i + 1]; ++k) cross += d.dep_col[k] / tile_rows != i / tile_rows;
+    const long long total = (long long)d.dep_col.size();
+    levels_form = total > 0 && 2 * cross > total;
+    if (const char* e = getenv("GBLAP_TRI_FORM")) {
+      if (!strcmp(e, "levels")) levels_form = true;
+      if (!strcmp(e, "tiles")) levels_form = false;
+    }
+  }
+  const int ntiles = levels_form ? 0 : (n + tile_rows - 1) / tile_rows;
   std::vector<int> tr0, tr1, tile_rec{0}, rec_flags;
   std::vector<RecDesc> recs;
-  std::vector<int> llev(tile_rows), bptr, bucket;
+  std::vector<int> llev(levels_form ? 1 : tile_rows), bptr, bucket;
   int nlvl = 0;
+  // rows of one level -> records (LONG rows alone, longest first; SHORT rows
+  // packed up to kTriRecRows per record and the slot size)
+  auto pack = [&](std::vector<int>& rows, int wait_for) {
+    std::stable_sort(rows.begin(), rows.end(), [&](int a, int b) { return deps_of(a) > deps_of(b); });
+    size_t p = 0;
+    while (p < rows.size() && deps_of(rows[p]) > kLongDeps) {
+      RecDesc r;
+      r.wait_for = wait_for;
+      r.is_long = true;
+      r.len = deps_of(rows[p]);
+      r.rows = {rows[p]};
+      recs.push_back(r);
+      ++p;
+    }
+    while (p < rows.size()) {
+      RecDesc r;
+      r.wait_for = wait_for;
+      r.is_long = false;
+      r.len = deps_of(rows[p]);
+      r.rows.push_back(rows[p++]);  // a SHORT row (<= kLongDeps deps) always fits a slot
+      while (p < rows.size() && (int)r.rows.size() < kTriRecRows &&
+             rec_size((int)r.rows.size() + 1, r.len, 8) <= kTriSlotBytes) {
+        r.rows.push_back(rows[p]);
+        ++p;
+      }
+      recs.push_back(r);
+    }
+  };
+  if (levels_form) {
+    std::vector<int> lptr(nlev + 1, 0), byl(n);
+    for (int i = 0; i < n; ++i) lptr[lev[i] + 1]++;
+    for (int l = 0; l < nlev; ++l) lptr[l + 1] += lptr[l];
+    {
+      std::vector<int> fill(lptr.begin(), lptr.end() - 1);
+      for (int i = 0; i < n; ++i) byl[fill[lev[i]]++] = i;
+    }
+    for (int l = 0; l < nlev; ++l) {
+      std::vector<int> rows(byl.begin() + lptr[l], byl.begin() + lptr[l + 1]);
+      pack(rows, 0);  // no tile-local dependencies: nothing to wait for in the tile
+    }
+    for (size_t r0 = 0; r0 < recs.size(); r0 += kLevelTileRecs) {
+      tr0.push_back(0);
+      tr1.push_back(0);
+      tile_rec.push_back((int)std::min(recs.size(), r0 + kLevelTileRecs));
+    }
+    nlvl = nlev;
+  }
   for (int q = 0; q < ntiles; ++q) {
     const int tix = lower ? q : ntiles - 1 - q;
     const int t0 = tix * tile_rows, t1 = std::min(n, t0 + tile_rows);
@@ -200,31 +270,7 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
     for (int l = 0; l < nl; ++l) {
       std::vector<int> rows(bucket.begin() + bptr[l], bucket.begin() + bptr[l + 1]);
       // longest first, so records group rows of similar length
-      std::stable_sort(rows.begin(), rows.end(), [&](int a, int b) { return deps_of(a) > deps_of(b); });
-      const int wait_for = (int)(recs.size() - tile_first);  // every earlier level of the tile
-      size_t p = 0;
-      while (p < rows.size() && deps_of(rows[p]) > kLongDeps) {
-        RecDesc r;
-        r.wait_for = wait_for;
-        r.is_long = true;
-        r.len = deps_of(rows[p]);
-        r.rows = {rows[p]};
-        recs.push_back(r);
-        ++p;
-      }
-      while (p < rows.size()) {
-        RecDesc r;
-        r.wait_for = wait_for;
-        r.is_long = false;
-        r.len = deps_of(rows[p]);
-        r.rows.push_back(rows[p++]);  // a SHORT row (<= kLongDeps deps) always fits a slot
-        while (p < rows.size() && (int)r.rows.size() < kTriRecRows &&
-               rec_size((int)r.rows.size() + 1, r.len, 8) <= kTriSlotBytes) {
-          r.rows.push_back(rows[p]);
-          ++p;
-        }
-        recs.push_back(r);
-      }
+      pack(rows, (int)(recs.size() - tile_first));  // waits for every earlier level of the tile
     }
     tile_rec.push_back((int)recs.size());
   }
@@ -250,8 +296,9 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
   plan->n = n;
   plan->lower = lower;
   plan->nlevels = nlev;
-  plan->tile_rows = tile_rows;
-  plan->ntiles = ntiles;
+  plan->tile_rows = levels_form ? 0 : tile_rows;
+  plan->ntiles = (int)tr0.size();
+  plan->levels_form = levels_form;
   plan->nlvl = nlvl;
   plan->nrec = (int)recs.size();
   plan->ndeps = (long long)d.dep_col.size();
