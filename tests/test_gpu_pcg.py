@@ -359,7 +359,11 @@ for name in ["grid2d", "grid3d", "chunglu", "knn", "aniso"]:
                                (uia, uja, ua, L.cuda_upper_triangular_solve, "usolve")):
         dp, dj, dv, y = dev(p), dev(j), dev(v), dev(np.zeros(n))
         fn(n, len(j), gb.ptr(dp), gb.ptr(dj), gb.ptr(dv), 0, gb.ptr(xs), gb.ptr(y))
-        ok = ok and bool(np.array_equal(y.cpu().numpy(), g[name + "_" + key]))
+        got, want = y.cpu().numpy(), g[name + "_" + key]
+        if name == "chunglu":  # rows of > 32 dependencies are reduced by a whole warp
+            ok = ok and bool(np.allclose(got, want, rtol=1e-12, atol=1e-14 * np.abs(want).max()))
+        else:
+            ok = ok and bool(np.array_equal(got, want))
     out["exact"][name] = ok
     A = gen.CSR(n, ia, ja, a)
     for prec in ("ichol", "GS_std"):
@@ -386,7 +390,9 @@ json.dump(out, open(sys.argv[2] + ".json", "w"))
 def test_levels_form(tmp_path):
     """The levels form of the triangular solves (records in global level
     order, every dependency through L2; chosen for random labellings) forced
-    on every case: the exact solves stay bit-identical to the reference's,
+    on every case: the exact solves stay bit-identical to the reference's
+    (to 1e-12 where rows of more than 32 dependencies are warp-reduced, as
+    in the tile form),
     PCG matches the oracle (iterations +-2%, x within 1e-6), and on a
     Chung-Lu graph both forms give the same solutions to the solve's
     accuracy."""
