@@ -237,7 +237,7 @@ __device__ __forceinline__ void wait_level(const int* s_done, int need, int* err
 // completion is published before the global stores.
 constexpr int kTriHeld = 4;       // dependencies held in registers per row
 constexpr int kTriTailBatch = 8;  // loads in flight per row beyond the held ones
-constexpr int kTriLongBatch = 4;  // loads in flight per lane in a LONG record
+constexpr int kTriLongBatch = 8;  // loads in flight per lane in a LONG record
 
 // Link of a tile to its neighbours inside a thread-block cluster: `in` is
 // this CTA's inbox (shared memory) holding the previous tile's rows
@@ -335,17 +335,32 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
   T yv = T(0);
   if (lng) {
     // lane-strided over the row; each lane issues kTriLongBatch loads before
-    // it consumes them (same per-lane order as one at a time)
+    // it consumes them (same per-lane order as one at a time), and the next
+    // batch's indices and values are in flight while this batch's values
+    // are awaited: a power-law hub row has tens of thousands of entries
     T s = T(0);
+    int cn[kTriLongBatch];
+    T ln[kTriLongBatch];
+#pragma unroll
+    for (int u = 0; u < kTriLongBatch; ++u) {
+      const int k = lane + 32 * u;
+      cn[u] = k < h.len ? __ldg(A.long_col + h.off + k) : -1;
+      ln[u] = cn[u] >= 0 ? __ldg(A.long_val + h.off + k) : T(0);
+    }
     for (int k0 = lane; k0 < h.len; k0 += 32 * kTriLongBatch) {
       int cb[kTriLongBatch];
       T lb[kTriLongBatch], vb[kTriLongBatch];
 #pragma unroll
       for (int u = 0; u < kTriLongBatch; ++u) {
-        const int k = k0 + 32 * u;
-        cb[u] = k < h.len ? __ldg(A.long_col + h.off + k) : -1;
-        lb[u] = cb[u] >= 0 ? __ldg(A.long_val + h.off + k) : T(0);
+        cb[u] = cn[u];
+        lb[u] = ln[u];
         vb[u] = cb[u] < 0 ? T(0) : (cb[u] >= t0 && cb[u] < t1) ? sy[cb[u] - t0] : other_tile_read(A, L, cb[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < kTriLongBatch; ++u) {  // the next batch's indices, in flight meanwhile
+        const int k = k0 + 32 * kTriLongBatch + 32 * u;
+        cn[u] = k < h.len ? __ldg(A.long_col + h.off + k) : -1;
+        ln[u] = cn[u] >= 0 ? __ldg(A.long_val + h.off + k) : T(0);
       }
 #pragma unroll
       for (int u = 0; u < kTriLongBatch; ++u) {
