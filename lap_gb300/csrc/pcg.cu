@@ -236,6 +236,7 @@ __global__ void __launch_bounds__(kThreads)
 // type in the split recurrence); also pre-fills the upper solve's output.
 template <typename T, typename TR>
 struct OpSplitLower {
+  static constexpr bool kPollValues = true;
   const TR* r;
   T* sfill;
   PcgState* st;
