@@ -248,17 +248,21 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
     const int t0 = tix * tile_rows, t1 = std::min(n, t0 + tile_rows);
     tr0.push_back(t0);
     tr1.push_back(t1);
-    int nl = 0;
-    for (int s = 0; s < t1 - t0; ++s) {
-      const int i = lower ? t0 + s : t1 - 1 - s;
-      int l = 0;
-      for (int k = d.row_ptr[i]; k < d.row_ptr[i + 1]; ++k) {
-        const int c = d.dep_col[k];
-        if (c >= t0 && c < t1) l = std::max(l, llev[c - t0] + 1);
-      }
-      llev[i - t0] = l;
-      nl = std::max(nl, l + 1);
+    // Rows of the tile in GLOBAL level order.  A row's dependencies all have
+    // lower global levels, so the in-tile ones sit in earlier buckets; and
+    // where a tile splits the dependency structure (a 96^3 grid's 9216-row
+    // planes in 8192-row tiles), a row's place in the tile also follows the
+    // dependencies in other tiles, which levels counted inside the tile alone
+    // would ignore -- those put rows that wait on a late other tile ahead of
+    // rows that could run (20x slower at 96^3).  On aligned tiles the two
+    // orders agree.
+    int lmin = nlev, lmax = -1;
+    for (int i = t0; i < t1; ++i) {
+      lmin = std::min(lmin, lev[i]);
+      lmax = std::max(lmax, lev[i]);
     }
+    const int nl = lmax - lmin + 1;
+    for (int i = t0; i < t1; ++i) llev[i - t0] = lev[i] - lmin;
     nlvl += nl;
     bptr.assign(nl + 1, 0);
     for (int i = t0; i < t1; ++i) bptr[llev[i - t0] + 1]++;
