@@ -52,12 +52,12 @@ struct SpmvPlan {
 // Tiled level schedule of one triangular factor (see tri_kernel.cuh).  Rows
 // are cut into contiguous tiles of tile_rows rows, processed in dependency
 // order (ascending for a lower factor, descending for an upper one).  Inside
-// a tile, rows are grouped by their level among the tile's own rows, and each
-// level into 32-row slices: a SHORT slice holds one row per lane with its
+// a tile, rows are grouped by their global level (dependency depth in the
+// whole factor), and each level into 32-row slices: a SHORT slice holds one row per lane with its
 // dependencies column-major (entry k of lane l at ent + k*32 + l); a LONG
 // slice holds one row with more than 32 dependencies, contiguous, reduced by
 // a whole warp.
-// Each tile-local level is stored as one or more RECORDS (tri_kernel.cuh):
+// Each level of a tile is stored as one or more RECORDS (tri_kernel.cuh):
 // a 16-byte header, the rows, their diagonal and its reciprocal, and the
 // dependency columns and values column-major -- contiguous and 16-byte
 // aligned so one TMA bulk copy stages a record in shared memory.  The FP64
@@ -84,7 +84,7 @@ struct TriPlan {
   // order with no rows of their own (every dependency is read through L2);
   // chosen when contiguous row tiles would hold few of the dependencies
   bool levels_form = false;
-  int nlvl = 0;              // tile-local levels, summed over tiles
+  int nlvl = 0;              // levels spanned by each tile, summed over tiles
   int nrec = 0;
   long long ndeps = 0;       // dependencies without padding (algorithmic size)
   int *tile_row0 = nullptr, *tile_row1 = nullptr;  // [ntiles], processing order

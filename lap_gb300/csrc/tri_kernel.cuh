@@ -10,8 +10,8 @@
 // of its FP32 rate, so every FP64 instruction on the dependency chain counts.
 //
 // Schedule (TriPlan, built on the host): rows are cut into contiguous tiles;
-// inside a tile rows are ordered by their level with respect to the tile's
-// own rows and packed into RECORDS of at most 32 rows of one level (rows,
+// inside a tile rows are ordered by their global level (dependency depth in
+// the whole factor) and packed into RECORDS of at most 32 rows of one level (rows,
 // diagonal, its reciprocal, dependency columns and values column-major;
 // contiguous and 16-byte aligned).  One CTA solves one tile at a time:
 //   * a producer warp streams the tile's records into a ring of shared-
