@@ -246,12 +246,38 @@ constexpr int kTriLongBatch = 8;  // loads in flight per lane in a LONG record
 // [in0, in1), pushed there by the CTA that solves them; `out` is the
 // shared::cluster address of the next CTA's inbox (0: none).  Without a
 // cluster both are empty and every other-tile value comes through L2.
+//
+// FP64 tiles leave no room for an inbox; their clusters PULL instead:
+// `in_remote` is the shared::cluster address of the previous tile's own
+// solution array in its CTA, polled there (sentinel as flag).
 template <typename T>
 struct TriLink {
   const T* in = nullptr;
   int in0 = 0, in1 = 0;
   uint32_t out = 0;
+  uint32_t in_remote = 0;
 };
+
+__device__ __forceinline__ float ld_cluster_relaxed(uint32_t addr, float*) {
+  float v;
+  asm volatile("ld.relaxed.cluster.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ double ld_cluster_relaxed(uint32_t addr, double*) {
+  double v;
+  asm volatile("ld.relaxed.cluster.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
+  return v;
+}
+// Polls a value in another CTA of the cluster; bounded like every wait.
+template <typename T>
+__device__ __noinline__ T wait_remote_slow(uint32_t addr, int* err) {
+  SpinClock clk;
+  for (unsigned polls = 1;; ++polls) {
+    const T v = ld_cluster_relaxed(addr, (T*)nullptr);
+    if (!is_sentinel(v)) return v;
+    if ((polls & 255u) == 0u && clk.expired(err)) return (T)__int_as_float(0x7FC00000);
+  }
+}
 
 __device__ __forceinline__ void st_cluster(uint32_t addr, float v) {
   asm volatile("st.relaxed.cluster.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
@@ -265,11 +291,15 @@ __device__ __forceinline__ void st_cluster(uint32_t addr, double v) {
 template <typename T>
 __device__ __forceinline__ T other_tile_read(const TriArgs<T>& A, const TriLink<T>& L, int c) {
   if (L.in && c >= L.in0 && c < L.in1) return *(const volatile T*)(L.in + (c - L.in0));
+  if (L.in_remote && c >= L.in0 && c < L.in1)
+    return ld_cluster_relaxed(L.in_remote + (uint32_t)(c - L.in0) * (uint32_t)sizeof(T), (T*)nullptr);
   return ld_relaxed(A.y + c);
 }
 template <typename T>
 __device__ __forceinline__ T other_tile_wait(const TriArgs<T>& A, const TriLink<T>& L, int c) {
   if (L.in && c >= L.in0 && c < L.in1) return wait_local_slow(L.in + (c - L.in0), A.err);
+  if (L.in_remote && c >= L.in0 && c < L.in1)
+    return wait_remote_slow<T>(L.in_remote + (uint32_t)(c - L.in0) * (uint32_t)sizeof(T), A.err);
   return wait_value_slow(A.y + c, A.err);
 }
 
@@ -390,7 +420,7 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
     if (lane == 0) {
       const T r = sub_rn(acc, s);
       yv = publishable(EXACT ? div_rn(r, diag[0]) : r * dinv[0]);
-      if (row >= t0 && row < t1) sy[row - t0] = yv;  // the levels form has no tile rows
+      if (row >= t0 && row < t1) st_shared_volatile(sy + (row - t0), yv);  // the levels form has no tile rows
     }
   } else if (act) {
     // tile-local values: complete (earlier tile-levels) or polled; all loads at once
@@ -429,7 +459,7 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
       }
     }
     yv = publishable(EXACT ? div_rn(acc, dg) : acc);
-    if (row >= t0 && row < t1) sy[row - t0] = yv;  // the levels form has no tile rows
+    if (row >= t0 && row < t1) st_shared_volatile(sy + (row - t0), yv);  // the levels form has no tile rows
   }
   __syncwarp();
   if (lane == 0) red_release_cta_add(s_done, 1);
@@ -529,15 +559,28 @@ __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArg
       const int g = s_tile;
       if ((long long)g * CL >= A.ntiles) break;  // the same for the whole cluster
       k = g * CL + (int)rank;                    // >= ntiles: idle in this group
+      constexpr bool kPull = sizeof(T) == 8;  // FP64: no room for an inbox
       if (k < A.ntiles && rank > 0) {
-        link.in = inbox;
         link.in0 = __ldg(A.tile_row0 + k - 1);
         link.in1 = __ldg(A.tile_row1 + k - 1);
-        for (int i = threadIdx.x; i < link.in1 - link.in0; i += kTriThreads) inbox[i] = sentinel<T>();
+        if constexpr (kPull) {
+          link.in_remote = cluster_map(sy, rank - 1);
+        } else {
+          link.in = inbox;
+          for (int i = threadIdx.x; i < link.in1 - link.in0; i += kTriThreads) inbox[i] = sentinel<T>();
+        }
       }
-      if (k + 1 < A.ntiles && rank + 1 < (unsigned)CL) link.out = cluster_map(inbox, rank + 1);
+      if constexpr (kPull) {
+        // the successor polls this tile's array from the barrier on
+        if (k < A.ntiles) {
+          const int rows = __ldg(A.tile_row1 + k) - __ldg(A.tile_row0 + k);
+          for (int i = threadIdx.x; i < rows; i += kTriThreads) sy[i] = sentinel<T>();
+        }
+      } else {
+        if (k + 1 < A.ntiles && rank + 1 < (unsigned)CL) link.out = cluster_map(inbox, rank + 1);
+      }
       __syncthreads();
-      cluster_sync_all();  // every inbox holds the sentinel before any push
+      cluster_sync_all();  // every inbox (or pulled array) holds the sentinel before any value
     } else {
       if (threadIdx.x == 0) s_tile = (int)atomicAdd(&A.ticket[0], 1u);
       __syncthreads();
@@ -640,6 +683,8 @@ int tri_blocks_per_sm();
 // CTAs per cluster for FP32 solves: -1 automatic (16, 8 or 4), 0 per-CTA
 // form, 4, 8 or 16 forced (GBLAP_TRI_CLUSTER)
 int tri_cluster_size();
+// FP64 solves in pulling clusters (GBLAP_TRI_FP64_CLUSTER=0 turns them off)
+bool tri_fp64_clusters();
 
 // GB_NOT_SUPPORTED when the device cannot place one cluster of CL CTAs, or,
 // with all_resident, cannot place every group's cluster at once.
@@ -708,6 +753,16 @@ int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   if (p.ntiles <= 0) return GB_OK;
   const size_t smem = (size_t)kTriSlots * kTriSlotBytes + (size_t)p.tile_rows * sizeof(T);
   if (smem > (size_t)kTriMaxDynSmem) return GB_NOT_SUPPORTED;  // an FP32-only plan in FP64
+  if constexpr (sizeof(T) == 8) {
+    // FP64: clusters that pull the previous tile's values (no inbox)
+    const int want = tri_cluster_size();
+    if (p.ntiles > 1 && !p.levels_form && want != 0 && tri_fp64_clusters()) {
+      int rc = GB_NOT_SUPPORTED;
+      if (want == 16 || want < 0) rc = tri_launch_cl<T, OP, EXACT, 16>(p, A, op, s, smem);
+      if (rc == GB_NOT_SUPPORTED && want != 16) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem);
+      if (rc != GB_NOT_SUPPORTED) return rc;
+    }
+  }
   if constexpr (sizeof(T) == 4) {
     const size_t smem_cl = smem + (size_t)p.tile_rows * sizeof(T);
     const int want = tri_cluster_size();

@@ -451,6 +451,15 @@ int tri_cluster_size() {
   return v;
 }
 
+bool tri_fp64_clusters() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("GBLAP_TRI_FP64_CLUSTER");
+    v = e && atoi(e) == 0 ? 0 : 1;
+  }
+  return v != 0;
+}
+
 int tri_grid(int ntiles) {
   return std::max(1, std::min(ntiles, device_sm_count() * tri_blocks_per_sm()));
 }

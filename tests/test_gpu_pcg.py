@@ -305,7 +305,7 @@ from lap_gb300 import gen
 A, b = gen.grid3d_lognormal(40, seed=1002)
 for prec in ("ichol", "GS_std"):
     s = gb.System.from_csr(A, prec)
-    for p in (1, 2):
+    for p in (0, 1, 2):
         x, r = s.solve(torch.from_numpy(b).cuda(), tol=1e-9, maxit=5000, precision=p)
         np.save(f"{sys.argv[2]}_{prec}_{p}.npy", x.cpu().numpy())
     s.close()
@@ -313,11 +313,12 @@ for prec in ("ichol", "GS_std"):
 
 
 def test_cluster_form_matches_per_cta_form(tmp_path):
-    """The FP32 solves in thread-block clusters pass boundary values through
-    distributed shared memory instead of L2: the arithmetic is the same, so
-    the mixed-precision solutions must be bitwise identical to the per-CTA
-    form's (GBLAP_TRI_CLUSTER=0), in clusters of 8 and of 16 alike.  The
-    switch is read once per process."""
+    """The solves in thread-block clusters pass boundary values through
+    distributed shared memory instead of L2 -- pushed into an inbox (FP32)
+    or pulled from the previous tile's CTA (FP64): the arithmetic is the
+    same, so every precision mode's solution must be bitwise identical to
+    the per-CTA form's (GBLAP_TRI_CLUSTER=0), in clusters of 8 and of 16
+    alike.  The switch is read once per process."""
     import os
     import subprocess
     import sys
@@ -331,7 +332,7 @@ def test_cluster_form_matches_per_cta_form(tmp_path):
                        timeout=600)
         out[mode] = stem
     for prec in ("ichol", "GS_std"):
-        for p in (1, 2):
+        for p in (0, 1, 2):
             a = np.load(f"{out['0']}_{prec}_{p}.npy")
             for cl in ("8", "16"):
                 c = np.load(f"{out[cl]}_{prec}_{p}.npy")
