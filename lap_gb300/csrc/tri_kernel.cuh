@@ -503,7 +503,7 @@ __device__ __forceinline__ int ld_cluster_s32(uint32_t addr) {
 // per group: after the group is known, after every inbox holds the
 // sentinel (before any push), and at the end (no CTA refills or frees its
 // inbox while its predecessor may still push into it).
-template <typename T, typename OP, bool EXACT, int CL = 1>
+template <typename T, typename OP, bool EXACT, int CL = 1, bool PULL = false>
 __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArgs<T> A, OP op) {
   constexpr int kTriConsumers = TriCons<T>::n;
   constexpr int kTriThreads = TriCons<T>::threads;
@@ -559,7 +559,7 @@ __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArg
       const int g = s_tile;
       if ((long long)g * CL >= A.ntiles) break;  // the same for the whole cluster
       k = g * CL + (int)rank;                    // >= ntiles: idle in this group
-      constexpr bool kPull = sizeof(T) == 8;  // FP64: no room for an inbox
+      constexpr bool kPull = PULL;  // no room for an inbox beside the tile
       if (k < A.ntiles && rank > 0) {
         link.in0 = __ldg(A.tile_row0 + k - 1);
         link.in1 = __ldg(A.tile_row1 + k - 1);
@@ -688,10 +688,10 @@ bool tri_fp64_clusters();
 
 // GB_NOT_SUPPORTED when the device cannot place one cluster of CL CTAs, or,
 // with all_resident, cannot place every group's cluster at once.
-template <typename T, typename OP, bool EXACT, int CL>
+template <typename T, typename OP, bool EXACT, int CL, bool PULL = false>
 int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, size_t smem,
                   bool all_resident = false) {
-  auto kern = tri_tile_kernel<T, OP, EXACT, CL>;
+  auto kern = tri_tile_kernel<T, OP, EXACT, CL, PULL>;
   static bool attr_set = false;  // one per instantiation
   if (!attr_set) {
     GB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kTriMaxDynSmem));
@@ -753,18 +753,20 @@ int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   if (p.ntiles <= 0) return GB_OK;
   const size_t smem = (size_t)kTriSlots * kTriSlotBytes + (size_t)p.tile_rows * sizeof(T);
   if (smem > (size_t)kTriMaxDynSmem) return GB_NOT_SUPPORTED;  // an FP32-only plan in FP64
-  if constexpr (sizeof(T) == 8) {
-    // FP64: clusters that pull the previous tile's values (no inbox)
+  const size_t smem_inbox = smem + (size_t)p.tile_rows * sizeof(T);
+  if (sizeof(T) == 8 || smem_inbox > (size_t)kTriMaxDynSmem) {
+    // clusters that pull the previous tile's values (no room for an inbox):
+    // every FP64 tile, and FP32 tiles taller than half the shared memory
     const int want = tri_cluster_size();
-    if (p.ntiles > 1 && !p.levels_form && want != 0 && tri_fp64_clusters()) {
+    if (p.ntiles > 1 && !p.levels_form && want != 0 && (sizeof(T) == 4 || tri_fp64_clusters())) {
       int rc = GB_NOT_SUPPORTED;
-      if (want == 16 || want < 0) rc = tri_launch_cl<T, OP, EXACT, 16>(p, A, op, s, smem);
-      if (rc == GB_NOT_SUPPORTED && want != 16) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem);
+      if (want == 16 || want < 0) rc = tri_launch_cl<T, OP, EXACT, 16, true>(p, A, op, s, smem);
+      if (rc == GB_NOT_SUPPORTED && want != 16) rc = tri_launch_cl<T, OP, EXACT, 8, true>(p, A, op, s, smem);
       if (rc != GB_NOT_SUPPORTED) return rc;
     }
   }
   if constexpr (sizeof(T) == 4) {
-    const size_t smem_cl = smem + (size_t)p.tile_rows * sizeof(T);
+    const size_t smem_cl = smem_inbox;
     const int want = tri_cluster_size();
     if (p.ntiles > 1 && !p.levels_form && smem_cl <= (size_t)kTriMaxDynSmem && want != 0) {
       int rc = GB_NOT_SUPPORTED;
