@@ -516,7 +516,8 @@ def run_ours(args, world, rank, local):
                             "rel_true_res": r_f32k["rel_true_res"]},
             "speedup_mixed_vs_fp64": round(v64 / v, 3),
             "solves_per_s_all_gpus": round(world * 1e3 / v, 3),
-            "e2e": {"value": round(ve2e, 4), "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * n,
+            "e2e": {"value": round(ve2e, 4), "unit": UNIT, "steps_ms": [round(v, 2) for v in e2e],
+                    "h2d_bytes_per_step": 2 * 8 * n,
                     "d2h_bytes_per_step": 8 * n},
             "roofline": roofline, "roofline_bandwidth_kernels": bw, "kernels": kernels,
             "gpu_launches": launches_mixed * args.steps,
