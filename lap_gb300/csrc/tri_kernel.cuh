@@ -97,6 +97,7 @@ struct TriArgs {
   unsigned* ticket;  // [0] next tile, [1] finished tiles, [2] exited blocks
   int* err;
   int tile_rows;
+  int poll;  // the plan's levels hold several records: lower solves poll values (see op_polls_values)
 };
 
 __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
@@ -306,9 +307,12 @@ __device__ __forceinline__ T other_tile_wait(const TriArgs<T>& A, const TriLink<
 // An OP with `static constexpr bool kPollValues = true` has its rows read
 // their tile-local dependencies by polling the values (sentinel as flag)
 // instead of first waiting for every earlier tile-level to be counted
-// complete: no release/acquire pair on the chain, but every lane polls its
-// own addresses.  Measured per solve on 128^3: faster for the lower solves,
-// slower for the upper ones, which keep the level counter.
+// complete -- when the plan's levels hold several records each (A.poll):
+// no release/acquire pair on the chain, but every lane polls its own
+// addresses.  Measured: the 128^3 lower solve 284 vs 308 us; where a level
+// is one record (8-row tiles of a 1024^2 grid) 1522 vs 1052 us, so such
+// plans keep the counter; upper solves keep it everywhere (128^3: 480 vs
+// 373 us).
 template <typename OP, typename = void>
 struct op_polls_values : std::false_type {};
 template <typename OP>
@@ -374,10 +378,10 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
       }
     }
   }
-  constexpr bool kPoll = op_polls_values<OP>::value;
+  const bool poll = op_polls_values<OP>::value && A.poll;  // uniform in the kernel
   // a tile-local value: complete once its level is counted, or polled
-  auto local = [&](int c) -> T { return kPoll ? wait_local(sy + (c - t0), A.err) : sy[c - t0]; };
-  if constexpr (!kPoll) wait_level(s_done, h.wait_for, A.err);
+  auto local = [&](int c) -> T { return poll ? wait_local(sy + (c - t0), A.err) : sy[c - t0]; };
+  if (!poll) wait_level(s_done, h.wait_for, A.err);
   T yv = T(0);
   if (lng) {
     // lane-strided over the row; each lane issues kTriLongBatch loads before

@@ -481,6 +481,7 @@ TriArgs<T> tri_args(const TriPlan& p, T* y, int* err, bool fma_form) {
   A.ticket = p.ticket;
   A.err = err;
   A.tile_rows = p.tile_rows;
+  A.poll = p.nlvl > 0 && 2 * p.nrec >= 3 * p.nlvl;  // at least 1.5 records per tile-level
   return A;
 }
 template TriArgs<double> tri_args<double>(const TriPlan&, double*, int*, bool);
