@@ -318,7 +318,7 @@ struct op_polls_values : std::false_type {};
 template <typename OP>
 struct op_polls_values<OP, std::void_t<decltype(OP::kPollValues)>> : std::bool_constant<OP::kPollValues> {};
 
-template <typename T, bool EXACT, typename OP>
+template <typename T, bool EXACT, bool POLL, typename OP>
 __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy, int t0, int t1,
                                              const unsigned char* rec, int lane, int* s_done,
                                              const TriLink<T>& L) {
@@ -378,10 +378,12 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
       }
     }
   }
-  const bool poll = op_polls_values<OP>::value && A.poll;  // uniform in the kernel
   // a tile-local value: complete once its level is counted, or polled
-  auto local = [&](int c) -> T { return poll ? wait_local(sy + (c - t0), A.err) : sy[c - t0]; };
-  if (!poll) wait_level(s_done, h.wait_for, A.err);
+  auto local = [&](int c) -> T {
+    if constexpr (POLL) return wait_local(sy + (c - t0), A.err);
+    else return sy[c - t0];
+  };
+  if constexpr (!POLL) wait_level(s_done, h.wait_for, A.err);
   T yv = T(0);
   if (lng) {
     // lane-strided over the row; each lane issues kTriLongBatch loads before
@@ -507,7 +509,7 @@ __device__ __forceinline__ int ld_cluster_s32(uint32_t addr) {
 // per group: after the group is known, after every inbox holds the
 // sentinel (before any push), and at the end (no CTA refills or frees its
 // inbox while its predecessor may still push into it).
-template <typename T, typename OP, bool EXACT, int CL = 1, bool PULL = false>
+template <typename T, typename OP, bool EXACT, int CL = 1, bool PULL = false, bool POLL = false>
 __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArgs<T> A, OP op) {
   constexpr int kTriConsumers = TriCons<T>::n;
   constexpr int kTriThreads = TriCons<T>::threads;
@@ -639,7 +641,7 @@ __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArg
           const unsigned u = base + q;
           const int slot = u % kTriSlots;
           if (!failed && !mbar_wait(&full_bar[slot], (u / kTriSlots) & 1u, A.err)) failed = true;
-          if (!failed) solve_record<T, EXACT>(A, op, sy, t0, t1, ring + slot * kTriSlotBytes, lane, &s_done, link);
+          if (!failed) solve_record<T, EXACT, POLL>(A, op, sy, t0, t1, ring + slot * kTriSlotBytes, lane, &s_done, link);
           __syncwarp();
           // after a failure the slot is not released: its copy may still be in
           // flight, and the producer must not aim another copy at it
@@ -692,10 +694,10 @@ bool tri_fp64_clusters();
 
 // GB_NOT_SUPPORTED when the device cannot place one cluster of CL CTAs, or,
 // with all_resident, cannot place every group's cluster at once.
-template <typename T, typename OP, bool EXACT, int CL, bool PULL = false>
+template <typename T, typename OP, bool EXACT, int CL, bool PULL = false, bool POLL = false>
 int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, size_t smem,
                   bool all_resident = false) {
-  auto kern = tri_tile_kernel<T, OP, EXACT, CL, PULL>;
+  auto kern = tri_tile_kernel<T, OP, EXACT, CL, PULL, POLL>;
   static bool attr_set = false;  // one per instantiation
   if (!attr_set) {
     GB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kTriMaxDynSmem));
@@ -752,8 +754,8 @@ int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, 
 // way) 16 gave 177 ms per IC(0) split solve against 181 ms for 8.
 // Everything else runs the per-CTA form on a persistent grid of
 // min(tiles, SMs x resident CTAs).
-template <typename T, typename OP, bool EXACT>
-int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
+template <typename T, typename OP, bool EXACT, bool POLL>
+int tri_launch_form(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   if (p.ntiles <= 0) return GB_OK;
   const size_t smem = (size_t)kTriSlots * kTriSlotBytes + (size_t)p.tile_rows * sizeof(T);
   if (smem > (size_t)kTriMaxDynSmem) return GB_NOT_SUPPORTED;  // an FP32-only plan in FP64
@@ -764,8 +766,8 @@ int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
     const int want = tri_cluster_size();
     if (p.ntiles > 1 && !p.levels_form && want != 0 && (sizeof(T) == 4 || tri_fp64_clusters())) {
       int rc = GB_NOT_SUPPORTED;
-      if (want == 16 || want < 0) rc = tri_launch_cl<T, OP, EXACT, 16, true>(p, A, op, s, smem);
-      if (rc == GB_NOT_SUPPORTED && want != 16) rc = tri_launch_cl<T, OP, EXACT, 8, true>(p, A, op, s, smem);
+      if (want == 16 || want < 0) rc = tri_launch_cl<T, OP, EXACT, 16, true, POLL>(p, A, op, s, smem);
+      if (rc == GB_NOT_SUPPORTED && want != 16) rc = tri_launch_cl<T, OP, EXACT, 8, true, POLL>(p, A, op, s, smem);
       if (rc != GB_NOT_SUPPORTED) return rc;
     }
   }
@@ -774,18 +776,29 @@ int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
     const int want = tri_cluster_size();
     if (p.ntiles > 1 && !p.levels_form && smem_cl <= (size_t)kTriMaxDynSmem && want != 0) {
       int rc = GB_NOT_SUPPORTED;
-      if (want == 16) rc = tri_launch_cl<T, OP, EXACT, 16>(p, A, op, s, smem_cl);
-      else if (want == 8) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
-      else if (want == 4) rc = tri_launch_cl<T, OP, EXACT, 4>(p, A, op, s, smem_cl);
+      if (want == 16) rc = tri_launch_cl<T, OP, EXACT, 16, false, POLL>(p, A, op, s, smem_cl);
+      else if (want == 8) rc = tri_launch_cl<T, OP, EXACT, 8, false, POLL>(p, A, op, s, smem_cl);
+      else if (want == 4) rc = tri_launch_cl<T, OP, EXACT, 4, false, POLL>(p, A, op, s, smem_cl);
       else {
-        rc = p.ntiles > 8 ? tri_launch_cl<T, OP, EXACT, 16>(p, A, op, s, smem_cl) : GB_NOT_SUPPORTED;
-        if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 8>(p, A, op, s, smem_cl);
-        if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 4>(p, A, op, s, smem_cl);
+        rc = p.ntiles > 8 ? tri_launch_cl<T, OP, EXACT, 16, false, POLL>(p, A, op, s, smem_cl) : GB_NOT_SUPPORTED;
+        if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 8, false, POLL>(p, A, op, s, smem_cl);
+        if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 4, false, POLL>(p, A, op, s, smem_cl);
       }
       if (rc != GB_NOT_SUPPORTED) return rc;
     }
   }
-  return tri_launch_cl<T, OP, EXACT, 1>(p, A, op, s, smem);
+  return tri_launch_cl<T, OP, EXACT, 1, false, POLL>(p, A, op, s, smem);
+}
+
+// Lower-solve OPs poll tile values where the plan's levels hold several
+// records each (A.poll); the two forms are separate instantiations, since a
+// runtime switch in the record code measured slower in both.
+template <typename T, typename OP, bool EXACT>
+int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
+  if constexpr (op_polls_values<OP>::value) {
+    if (A.poll) return tri_launch_form<T, OP, EXACT, true>(p, A, op, s);
+  }
+  return tri_launch_form<T, OP, EXACT, false>(p, A, op, s);
 }
 
 template <typename T>
