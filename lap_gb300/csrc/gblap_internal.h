@@ -107,6 +107,11 @@ struct TriPlan {
   int *order = nullptr;
   int norder = 0;
   unsigned *ticket = nullptr;  // [0] next tile, [1] finished tiles, [2] exited blocks
+  // partial sums of split hub rows (one slot per partial record), FP64 and
+  // FP32 views, held at the sentinel between uses
+  int nslots = 0;
+  double *part64 = nullptr;
+  float *part32 = nullptr;
 };
 
 }  // namespace gb

@@ -70,6 +70,15 @@ constexpr int kTriRecTable = 1024;                     // records of a tile cach
 constexpr int kTriMaxDynSmem = 212 * 1024;             // ring + the largest tile (FP32 x 32768 rows)
 constexpr int kTriRecRows = 32;                        // rows per record (one per lane)
 constexpr int kRecLong = 2;                            // record flag: one row, warp-reduced
+// A row of more than kTriSplitDeps dependencies (a power-law hub) is split:
+// PART records reduce kTriPartDeps of its entries each (any warp) into a
+// slot, and a COMBINE record after them adds the slots in order and solves
+// the row.  Header: off = the part's first long entry, pad1 = its slot (the
+// combine's first slot), len = the part's entries (the combine's parts).
+constexpr int kRecPart = 4;
+constexpr int kRecCombine = 8;
+constexpr int kTriSplitDeps = 2048;
+constexpr int kTriPartDeps = 1024;
 
 // Record header (32 bytes).  Layout after it, R4 = nrows rounded up to 4:
 //   int rows[R4]; T diag[R4]; T dinv[R4]; int cols[len*R4]; T vals[len*R4]
@@ -97,6 +106,7 @@ struct TriArgs {
   unsigned* ticket;  // [0] next tile, [1] finished tiles, [2] exited blocks
   int* err;
   int tile_rows;
+  T* part;   // [plan nslots] partial sums of split rows (sentinel between uses)
   int poll;  // the plan's levels hold several records: lower solves poll values (see op_polls_values)
 };
 
@@ -391,6 +401,16 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
     // batch's indices and values are in flight while this batch's values
     // are awaited: a power-law hub row has tens of thousands of entries
     T s = T(0);
+    const bool part = (h.flags & kRecPart) != 0, comb = (h.flags & kRecCombine) != 0;
+    if (comb) {
+      // a split row: its parts' sums in part order (written by other warps)
+      if (lane == 0)
+        for (int k = 0; k < h.len; ++k) {
+          T v = ld_relaxed(A.part + h.pad1 + k);
+          if (is_sentinel(v)) v = wait_value_slow(A.part + h.pad1 + k, A.err);
+          s = k == 0 ? v : add_rn(s, v);
+        }
+    } else {
     int cn[kTriLongBatch];
     T ln[kTriLongBatch];
 #pragma unroll
@@ -423,7 +443,10 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
       }
     }
     s = warp_sum(s);
-    if (lane == 0) {
+    }
+    if (lane == 0 && part) {
+      st_relaxed(A.part + h.pad1, publishable(s));  // this part's sum, for the combine record
+    } else if (lane == 0) {
       const T r = sub_rn(acc, s);
       yv = publishable(EXACT ? div_rn(r, diag[0]) : r * dinv[0]);
       if (row >= t0 && row < t1) st_shared_volatile(sy + (row - t0), yv);  // the levels form has no tile rows
@@ -469,7 +492,7 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
   }
   __syncwarp();
   if (lane == 0) red_release_cta_add(s_done, 1);
-  if (act && (!lng || lane == 0)) {
+  if (act && (!lng || lane == 0) && !(h.flags & kRecPart)) {
     if (L.out) st_cluster(L.out + (uint32_t)(row - t0) * (uint32_t)sizeof(T), yv);  // next tile's inbox
     st_relaxed(A.y + row, yv);
     op.done(row, yv, dp);
@@ -795,6 +818,8 @@ int tri_launch_form(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s
 // runtime switch in the record code measured slower in both.
 template <typename T, typename OP, bool EXACT>
 int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
+  // split hub rows: every partial-sum slot at the sentinel before the solve
+  if (p.nslots > 0) GB_TRY(fill_sentinel_dev(p.nslots, A.part, s));
   if constexpr (op_polls_values<OP>::value) {
     if (A.poll) return tri_launch_form<T, OP, EXACT, true>(p, A, op, s);
   }

@@ -55,6 +55,8 @@ struct RecDesc {
   bool is_long;
   int len;
   std::vector<int> rows;
+  int part = -1;  // split row: >= 0 the part's index, -2 the combine record
+  int nparts = 0, slot0 = 0;
 };
 
 // Lays out all records in precision S; fills the RecordSet's host images.
@@ -66,6 +68,7 @@ void layout(const TriDeps& d, const std::vector<RecDesc>& recs, int S, std::vect
   buf.clear();
   off.clear();
   nbytes.clear();
+  int long_base = 0;  // the current long row's first entry in long_col
   vdst.clear();
   ddst.clear();
   idst.clear();
@@ -94,12 +97,25 @@ void layout(const TriDeps& d, const std::vector<RecDesc>& recs, int S, std::vect
     }
     if (r.is_long) {
       const int row = r.rows[0];
-      hdr[3] = long_col ? (int)long_col->size() : 0;
-      if (long_col)
-        for (int k = d.row_ptr[row]; k < d.row_ptr[row + 1]; ++k) {
-          long_col->push_back(d.dep_col[k]);
-          long_src->push_back(d.dep_src[k]);
-        }
+      if (r.part == -2) {  // combine: parts and first slot
+        hdr[1] = r.nparts;
+        hdr[2] = kRecLong | kRecCombine;
+        hdr[6] = r.slot0;
+        continue;
+      }
+      if (r.part <= 0) {  // a whole long row, or its first part: the row's entries
+        long_base = long_col ? (int)long_col->size() : 0;
+        if (long_col)
+          for (int k = d.row_ptr[row]; k < d.row_ptr[row + 1]; ++k) {
+            long_col->push_back(d.dep_col[k]);
+            long_src->push_back(d.dep_src[k]);
+          }
+      }
+      hdr[3] = long_base + (r.part > 0 ? r.part * kTriPartDeps : 0);
+      if (r.part >= 0) {
+        hdr[2] = kRecLong | kRecPart;
+        hdr[6] = r.slot0 + r.part;
+      }
       continue;
     }
     int* cols = reinterpret_cast<int*>(buf.data() + base + kRecHdrBytes + 4 * R4 + 2 * S * R4);
@@ -179,6 +195,7 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
   // would wait on many earlier tiles, and tiles not yet resident start only
   // when whole earlier tiles have finished.  GBLAP_TRI_FORM=tiles|levels
   // forces a form.
+  int nslots = 0;  // partial-sum slots of split hub rows
   bool levels_form = false;
   {
     long long cross = 0;
@@ -207,6 +224,21 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
       r.is_long = true;
       r.len = deps_of(rows[p]);
       r.rows = {rows[p]};
+      if (r.len > kTriSplitDeps) {  // a hub: parts on any warps, then the combine
+        const int np = (r.len + kTriPartDeps - 1) / kTriPartDeps;
+        for (int k = 0; k < np; ++k) {
+          RecDesc q = r;
+          q.part = k;
+          q.nparts = np;
+          q.slot0 = nslots;
+          q.len = std::min(kTriPartDeps, r.len - k * kTriPartDeps);
+          recs.push_back(q);
+        }
+        r.part = -2;
+        r.nparts = np;
+        r.slot0 = nslots;
+        nslots += np;
+      }
       recs.push_back(r);
       ++p;
     }
@@ -300,6 +332,14 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
   plan->n = n;
   plan->lower = lower;
   plan->nlevels = nlev;
+  plan->nslots = nslots;
+  if (nslots > 0) {
+    GB_CUDA_TRY(cudaMalloc(&plan->part64, sizeof(double) * nslots));
+    GB_CUDA_TRY(cudaMalloc(&plan->part32, sizeof(float) * nslots));
+    GB_TRY(fill_sentinel_dev(nslots, plan->part64, 0));
+    GB_TRY(fill_sentinel_dev(nslots, plan->part32, 0));
+    GB_CUDA_TRY(cudaDeviceSynchronize());
+  }
   plan->tile_rows = levels_form ? 0 : tile_rows;
   plan->ntiles = (int)tr0.size();
   plan->levels_form = levels_form;
@@ -325,8 +365,8 @@ void tri_plan_free(TriPlan* p) {
   free_set(&p->r64);
   free_set(&p->r32);
   if (p->buf64s) cudaFree(p->buf64s);
-  void* ptrs[] = {p->tile_row0, p->tile_row1, p->tile_rec, p->rec_flags, p->vsrc,
-                  p->dsrc,      p->long_col,  p->long_src, p->order,     p->ticket};
+  void* ptrs[] = {p->tile_row0, p->tile_row1, p->tile_rec, p->rec_flags, p->vsrc, p->dsrc,
+                  p->long_col,  p->long_src,  p->order,    p->ticket,    p->part64, p->part32};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   *p = TriPlan();
@@ -481,6 +521,8 @@ TriArgs<T> tri_args(const TriPlan& p, T* y, int* err, bool fma_form) {
   A.ticket = p.ticket;
   A.err = err;
   A.tile_rows = p.tile_rows;
+  if constexpr (sizeof(T) == 8) A.part = reinterpret_cast<T*>(p.part64);
+  else A.part = reinterpret_cast<T*>(p.part32);
   A.poll = p.nlvl > 0 && 2 * p.nrec >= 3 * p.nlvl;  // at least 1.5 records per tile-level
   return A;
 }
