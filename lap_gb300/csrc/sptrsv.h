@@ -34,7 +34,11 @@ int deps_ichol(int n, const int* ia, const int* ja, const std::vector<int>& tpos
 // shared memory only as FP32 and may be solved in FP32 only.
 constexpr int kTriMaxTileRows64 = 16384;
 constexpr int kTriMaxTileRows32 = 32768;
-int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows = 0);
+// level_run: records per run in the levels form (0: one per consumer warp
+// of an FP64 CTA; FP32 plans pass tri_consumer_warps(4))
+int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows = 0, int level_run = 0);
+// consumer warps of one triangular-solve CTA for elements of elem_bytes
+int tri_consumer_warps(int elem_bytes);
 int tri_default_tile_rows(int n);
 // Tile rows of the FP32-only plans: twice the FP64 default (32768 at most).
 int tri_default_tile_rows32(int n);

@@ -282,8 +282,8 @@ extern "C" int gb_system_create(int n, int nnz, const int* ia, const int* ja, co
     const bool t32_env = getenv("GBLAP_TRI_TILE_ROWS32") != nullptr;
     const int t32l = t32_env ? tri_default_tile_rows32(n) : tri_default_tile_rows(n);
     const int t32u = tri_default_tile_rows32(n);
-    CK(tri_plan_build(dl, &s->L32, t32l));
-    CK(tri_plan_build(du, &s->U32, t32u));
+    CK(tri_plan_build(dl, &s->L32, t32l, tri_consumer_warps(4)));
+    CK(tri_plan_build(du, &s->U32, t32u, tri_consumer_warps(4)));
   }
   if (prec == GB_PREC_IT_JACOBI || prec == GB_PREC_GS_IT || prec == GB_PREC_GS_IT2) {
     std::vector<int> lp(n + 1, 0), up(n + 1, 0), lj, uj, lm, um;

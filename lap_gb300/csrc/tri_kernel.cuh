@@ -70,14 +70,14 @@ constexpr int kTriRecTable = 1024;                     // records of a tile cach
 constexpr int kTriMaxDynSmem = 212 * 1024;             // ring + the largest tile (FP32 x 32768 rows)
 constexpr int kTriRecRows = 32;                        // rows per record (one per lane)
 constexpr int kRecLong = 2;                            // record flag: one row, warp-reduced
-// A row of more than kTriSplitDeps dependencies (a power-law hub) is split:
-// PART records reduce kTriPartDeps of its entries each (any warp) into a
-// slot, and a COMBINE record after them adds the slots in order and solves
-// the row.  Header: off = the part's first long entry, pad1 = its slot (the
+// A row of more than two parts' dependencies (a power-law hub; a part is
+// kTriPartDeps entries unless the plan is told otherwise) is split: PART
+// records reduce a part of its entries each (any warp) into a slot, and a
+// COMBINE record after them adds the slots in a fixed order and solves the
+// row.  Header: off = the part's first long entry, pad1 = its slot (the
 // combine's first slot), len = the part's entries (the combine's parts).
 constexpr int kRecPart = 4;
 constexpr int kRecCombine = 8;
-constexpr int kTriSplitDeps = 2048;
 constexpr int kTriPartDeps = 1024;
 
 // Record header (32 bytes).  Layout after it, R4 = nrows rounded up to 4:
@@ -403,13 +403,31 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
     T s = T(0);
     const bool part = (h.flags & kRecPart) != 0, comb = (h.flags & kRecCombine) != 0;
     if (comb) {
-      // a split row: its parts' sums in part order (written by other warps)
-      if (lane == 0)
-        for (int k = 0; k < h.len; ++k) {
-          T v = ld_relaxed(A.part + h.pad1 + k);
+      // a split row: its parts' sums (written by other warps), lane-strided
+      // and then the warp's fixed shuffle order, so the sum does not depend
+      // on which part finished first; all of a lane's loads are in flight
+      // before it waits on one
+      T pv[kTriLongBatch];
+#pragma unroll
+      for (int u = 0; u < kTriLongBatch; ++u) {
+        const int k = lane + 32 * u;
+        pv[u] = k < h.len ? ld_relaxed(A.part + h.pad1 + k) : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < kTriLongBatch; ++u) {
+        const int k = lane + 32 * u;
+        if (k < h.len) {
+          T v = pv[u];
           if (is_sentinel(v)) v = wait_value_slow(A.part + h.pad1 + k, A.err);
-          s = k == 0 ? v : add_rn(s, v);
+          s = add_rn(s, v);
         }
+      }
+      for (int k = lane + 32 * kTriLongBatch; k < h.len; k += 32) {
+        T v = ld_relaxed(A.part + h.pad1 + k);
+        if (is_sentinel(v)) v = wait_value_slow(A.part + h.pad1 + k, A.err);
+        s = add_rn(s, v);
+      }
+      s = warp_sum(s);
     } else {
     int cn[kTriLongBatch];
     T ln[kTriLongBatch];
@@ -760,7 +778,7 @@ int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, 
     }
     per_sm = per_sm < tri_blocks_per_sm() ? per_sm : tri_blocks_per_sm();
     const long long cap = (long long)device_sm_count() * per_sm;
-    const int grid = (int)(p.ntiles < cap ? p.ntiles : cap);
+    const int grid = (int)(A.ntiles < cap ? A.ntiles : cap);
     kern<<<grid, TriCons<T>::threads, smem, s>>>(A, op);
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;

@@ -40,8 +40,6 @@ namespace {
 // single row of kLongDeps dependencies must fit a ring slot:
 // header + 4*4 + 2*8*4 + kLongDeps*4*12 <= kTriSlotBytes.
 constexpr int kLongDeps = 32;
-// levels form: records per ticket (one CTA's run of records)
-constexpr int kLevelTileRecs = 128;
 static_assert(kRecHdrBytes + 16 + 64 + kLongDeps * 4 * 12 <= kTriSlotBytes, "record slot too small");
 
 // bytes of a SHORT record with `rows` rows of up to `len` dependencies
@@ -57,6 +55,7 @@ struct RecDesc {
   std::vector<int> rows;
   int part = -1;  // split row: >= 0 the part's index, -2 the combine record
   int nparts = 0, slot0 = 0;
+  int first = 0;  // a part: its first entry within the row
 };
 
 // Lays out all records in precision S; fills the RecordSet's host images.
@@ -111,7 +110,7 @@ void layout(const TriDeps& d, const std::vector<RecDesc>& recs, int S, std::vect
             long_src->push_back(d.dep_src[k]);
           }
       }
-      hdr[3] = long_base + (r.part > 0 ? r.part * kTriPartDeps : 0);
+      hdr[3] = long_base + (r.part > 0 ? r.first : 0);
       if (r.part >= 0) {
         hdr[2] = kRecLong | kRecPart;
         hdr[6] = r.slot0 + r.part;
@@ -156,7 +155,7 @@ void free_set(RecordSet* rs) {
 
 }  // namespace
 
-int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
+int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows, int level_run) {
   const int n = d.n;
   const bool lower = d.lower;
   if (tile_rows <= 0) tile_rows = tri_default_tile_rows(n);
@@ -190,7 +189,7 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
   // memory) when rows and their dependencies are near in index, as on grids.
   // When most dependencies cross tiles (a random labelling, power-law
   // graphs) the levels form takes over: records in global level order, cut
-  // into runs of kLevelTileRecs records that CTAs take by ticket; with no
+  // into runs of records (one per consumer warp) that CTAs take by ticket; with no
   // rows of their own, every dependency is read through L2.  Tiled, a tile
   // would wait on many earlier tiles, and tiles not yet resident start only
   // when whole earlier tiles have finished.  GBLAP_TRI_FORM=tiles|levels
@@ -208,6 +207,9 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
       if (!strcmp(e, "tiles")) levels_form = false;
     }
   }
+  // entries per part of a split hub row; rows of more than two parts split
+  int part_deps = kTriPartDeps;
+  if (const char* e = getenv("GBLAP_TRI_PART_DEPS")) part_deps = std::max(32, atoi(e));
   const int ntiles = levels_form ? 0 : (n + tile_rows - 1) / tile_rows;
   std::vector<int> tr0, tr1, tile_rec{0}, rec_flags;
   std::vector<RecDesc> recs;
@@ -224,14 +226,15 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
       r.is_long = true;
       r.len = deps_of(rows[p]);
       r.rows = {rows[p]};
-      if (r.len > kTriSplitDeps) {  // a hub: parts on any warps, then the combine
-        const int np = (r.len + kTriPartDeps - 1) / kTriPartDeps;
+      if (r.len > 2 * part_deps) {  // a hub: parts on any warps, then the combine
+        const int np = (r.len + part_deps - 1) / part_deps;
         for (int k = 0; k < np; ++k) {
           RecDesc q = r;
           q.part = k;
           q.nparts = np;
           q.slot0 = nslots;
-          q.len = std::min(kTriPartDeps, r.len - k * kTriPartDeps);
+          q.first = k * part_deps;
+          q.len = std::min(part_deps, r.len - k * part_deps);
           recs.push_back(q);
         }
         r.part = -2;
@@ -268,10 +271,17 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows) {
       std::vector<int> rows(byl.begin() + lptr[l], byl.begin() + lptr[l + 1]);
       pack(rows, 0);  // no tile-local dependencies: nothing to wait for in the tile
     }
-    for (size_t r0 = 0; r0 < recs.size(); r0 += kLevelTileRecs) {
+    // One record per consumer warp in each run: a level's records are
+    // mostly independent, and a warp solves its records one after another,
+    // so a run longer than the warps serialises a level on one CTA while
+    // the other CTAs wait on it (4.19M-row Chung-Lu, FP32 lower solve:
+    // 8.6 ms with runs of 128 records, 1.7 ms with 16).
+    size_t run = level_run > 0 ? level_run : TriCons<double>::n;
+    if (const char* e = getenv("GBLAP_TRI_LEVEL_RUN")) run = (size_t)std::max(1, atoi(e));
+    for (size_t r0 = 0; r0 < recs.size(); r0 += run) {
       tr0.push_back(0);
       tr1.push_back(0);
-      tile_rec.push_back((int)std::min(recs.size(), r0 + kLevelTileRecs));
+      tile_rec.push_back((int)std::min(recs.size(), r0 + run));
     }
     nlvl = nlev;
   }
@@ -499,6 +509,8 @@ bool tri_fp64_clusters() {
   }
   return v != 0;
 }
+
+int tri_consumer_warps(int elem_bytes) { return elem_bytes == 8 ? TriCons<double>::n : TriCons<float>::n; }
 
 int tri_grid(int ntiles) {
   return std::max(1, std::min(ntiles, device_sm_count() * tri_blocks_per_sm()));

@@ -425,12 +425,18 @@ def test_levels_form(tmp_path):
 
 
 @pytest.mark.parametrize("prec", ["ichol", "GS_std"])
-def test_split_hub_rows_match_oracle(prec):
-    """Rows of more than 2048 dependencies (three in each factor of this
-    65,475-row Chung-Lu graph, up to 6159) are solved as parts on several
-    warps plus a combine record: the PCG solution still matches the
-    reference's CPU PCG (oracle) within 1e-6 and its iteration count within
-    2%, in FP64 and in split precision (whose target is the same tol)."""
+@pytest.mark.parametrize("part_deps", [None, "32"])
+def test_split_hub_rows_match_oracle(prec, part_deps, monkeypatch):
+    """Rows of more than two parts of dependencies (with the default 1024-
+    entry parts, three in each factor of this 65,475-row Chung-Lu graph, up
+    to 6159) are solved as parts on several warps plus a combine record: the
+    PCG solution still matches the reference's CPU PCG (oracle) within 1e-6
+    and its iteration count within 2%, in FP64 and in split precision (whose
+    target is the same tol). 32-entry parts split every row of more than 64
+    dependencies and give the largest row 193 parts, which the combine reads
+    in several loads per lane."""
+    if part_deps:
+        monkeypatch.setenv("GBLAP_TRI_PART_DEPS", part_deps)
     A, b = gen.chung_lu(1 << 16, seed=1003)
     ref = oracle.solve(A.n, A.ia, A.ja, A.a, b, prec, 1e-10, 5000)
     s = gb.System.from_csr(A, prec)
