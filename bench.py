@@ -348,18 +348,26 @@ def run_workload(args, local):
             sg.close()
         line["one_by_one_device_ms"] = round(ms, 2)
         line["one_by_one_wall_s"] = round(time.time() - t2, 1)
-    elif wl == "multirhs32":
+    elif wl in ("multirhs32", "multirhs64"):
+        nr = int(wl[len("multirhs"):])
         A, _ = gen.grid3d_lognormal(128, seed=1002)
-        Bm = torch.from_numpy(gen.multi_rhs(A.n, 32, seed=1005)).cuda()
-        line["config"] = "128^3 lognormal Laplacian, 32 RHS, line_jacobi, tol 1e-8, one graph launch"
+        Bm = torch.from_numpy(gen.multi_rhs(A.n, nr, seed=1005)).cuda()
+        line["config"] = (f"128^3 lognormal Laplacian, {nr} RHS, line_jacobi, tol 1e-8, "
+                          + ("one graph launch" if nr <= 32 else "chunks of 32 RHS, one graph launch each"))
         sysm = gb.System.from_csr(A, "line_jacobi")
         X64, i64, _ = gb.solve_multi(sysm, Bm, tol=1e-8, maxit=20000, precision=0)
-        for p in (0, 2):
-            gb.solve_multi(sysm, Bm, tol=1e-8, maxit=20000, precision=p)
-            X, its, r = gb.solve_multi(sysm, Bm, tol=1e-8, maxit=20000, precision=p)
-            line[f"precision{p}"] = {"ms": round(r["device_ms"], 2), "max_iters": int(its.max()),
-                                     "flag": r["flag"], "rel_true_res_max": r["rel_true_res"],
-                                     "rel_err_vs_fp64": float(torch.linalg.norm(X - X64) / torch.linalg.norm(X64))}
+        forms = [("", None)] + ([("blocks_", "blocks")] if nr > 32 else [])
+        for tag, form in forms:
+            if form:  # every column in one launch on concatenated vectors
+                os.environ["GBLAP_MULTI_FORM"] = form
+            for p in (0, 2):
+                gb.solve_multi(sysm, Bm, tol=1e-8, maxit=20000, precision=p)
+                X, its, r = gb.solve_multi(sysm, Bm, tol=1e-8, maxit=20000, precision=p)
+                line[f"{tag}precision{p}"] = {
+                    "ms": round(r["device_ms"], 2), "max_iters": int(its.max()), "flag": r["flag"],
+                    "rel_true_res_max": r["rel_true_res"],
+                    "rel_err_vs_fp64": float(torch.linalg.norm(X - X64) / torch.linalg.norm(X64))}
+            os.environ.pop("GBLAP_MULTI_FORM", None)
         ms = 0.0
         for k in range(Bm.shape[0]):
             _, rs = sysm.solve(Bm[k], tol=1e-8, maxit=20000)
@@ -541,7 +549,7 @@ def main():
                     help="only the eager per-kernel profile of each precision mode (for ncu)")
     ap.add_argument("--profile-iters", type=int, default=3)
     ap.add_argument("--workload", default="ichol128",
-                    choices=["ichol128", "jacobi256", "chunglu4m", "batch512", "multirhs32", "adjoint1024",
+                    choices=["ichol128", "jacobi256", "chunglu4m", "batch512", "multirhs32", "multirhs64", "adjoint1024",
                              "mmread128"],
                     help="ichol128 is the headline line; the others are the remaining configurations")
     ap.add_argument("--fd-edges", type=int, default=16)

@@ -158,8 +158,11 @@ int gb_batch_solve(gb_batch batch, const double *b, double *x, const gb_pcg_opts
 
 /* Multi-RHS: nrhs right-hand sides on one system, B and X row-major
  * [nrhs][n] (X holds x0).  Each column runs its own PCG recurrence in the
- * batch engine above; the matrix is read once per iteration for all
- * columns.  Systems with "line_jacobi" or "none"; precision 0 or 2. */
+ * batch engine above; up to 32 columns share one read of the matrix per
+ * iteration (more run as consecutive chunks of 32 and a shorter last one;
+ * iters_host still receives every column's count and result aggregates
+ * all columns, device_ms summed over the chunks).  Systems with
+ * "line_jacobi" or "none"; precision 0 or 2. */
 int gb_pcg_solve_multi(gb_system sys, int nrhs, const double *B, double *X,
                        const gb_pcg_opts *opts, int *iters_host, gb_pcg_result *result);
 

@@ -6,7 +6,8 @@
 //   * multi-RHS: S right-hand sides on one gb_system (gb_pcg_solve_multi),
 //     the matrix shared and read once per iteration for all columns; up to
 //     32 right-hand sides run on interleaved vectors ([n][S], transposed on
-//     entry and exit), more on the concatenated layout.
+//     entry and exit), more as consecutive chunks of 32 and a shorter last
+//     one (the concatenated layout remains as GBLAP_MULTI_FORM=blocks).
 // Each system runs its own PCG recurrence of cg.c:42-126 -- its own alpha,
 // beta, rho, stopping test and flag -- held in one PcgState per system, so
 // the single-system building blocks (pcg_alpha, pcg_check) apply unchanged.
@@ -28,6 +29,7 @@
 // the single-system split solve, per system.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -1334,18 +1336,24 @@ void batch_release(gb_batch bt) {
 }
 }  // namespace gb
 
-extern "C" int gb_pcg_solve_multi(gb_system sys, int nrhs, const double* B, double* X,
-                                  const gb_pcg_opts* opts, int* iters_host, gb_pcg_result* result) {
-  if (!sys || nrhs <= 0 || !B || !X) return GB_BAD_INPUT;
-  if (sys->prec != GB_PREC_LINE_JACOBI && sys->prec != GB_PREC_NONE) return GB_NOT_SUPPORTED;
-  if ((long long)nrhs * sys->n >= (1LL << 31) - 1) return GB_NOT_SUPPORTED;
-  gb_batch bt = sys->multi;
-  // rebuilt when the count changes or the system's SpMV plan was rebuilt (autotuning)
+namespace {
+
+// More than this many right-hand sides run as consecutive interleaved
+// chunks: one lane per right-hand side in a warp.
+constexpr int kIlMaxRhs = 32;
+
+// The shared-matrix batch for nrhs columns in *slot: reused while the count
+// and the system's SpMV plan are unchanged, rebuilt otherwise (autotuning
+// rebuilds the plan).  interleaved = 0 gives the block form: the columns as
+// concatenated vectors, one bundle chunk per column.
+int multi_batch(gb_system sys, gb_batch* slot, int nrhs, bool interleaved, gb_batch* out) {
+  gb_batch bt = *slot;
   const bool stale = bt && (bt->bundles != sys->plan.bundles ||
-                            (bt->inter ? bt->nbun : bt->nb) != sys->plan.nbundles);
+                            (bt->inter ? bt->nbun : bt->nb) != sys->plan.nbundles ||
+                            (bt->inter != 0) != interleaved);
   if (!bt || bt->count != nrhs || stale) {
     if (bt) batch_free(bt);
-    sys->multi = nullptr;
+    *slot = nullptr;
     bt = new gb_batch_s();
     bt->count = nrhs;
     bt->shared = 1;
@@ -1359,7 +1367,7 @@ extern "C" int gb_pcg_solve_multi(gb_system sys, int nrhs, const double* B, doub
     bt->a32 = sys->a32;
     bt->d_r = sys->d_r;
     int rc = GB_OK;
-    if (nrhs <= 32) {
+    if (interleaved) {
       // interleaved vectors; partials per (right-hand side, warp) of a fixed grid
       bt->inter = 1;
       bt->bundles = sys->plan.bundles;
@@ -1389,7 +1397,56 @@ extern "C" int gb_pcg_solve_multi(gb_system sys, int nrhs, const double* B, doub
       batch_free(bt);
       return rc;
     }
-    sys->multi = bt;
+    *slot = bt;
   }
-  return batch_solve(bt, B, X, opts, iters_host, nullptr, result);
+  *out = bt;
+  return GB_OK;
+}
+
+}  // namespace
+
+extern "C" int gb_pcg_solve_multi(gb_system sys, int nrhs, const double* B, double* X,
+                                  const gb_pcg_opts* opts, int* iters_host, gb_pcg_result* result) {
+  if (!sys || nrhs <= 0 || !B || !X) return GB_BAD_INPUT;
+  if (sys->prec != GB_PREC_LINE_JACOBI && sys->prec != GB_PREC_NONE) return GB_NOT_SUPPORTED;
+  if ((long long)nrhs * sys->n >= (1LL << 31) - 1) return GB_NOT_SUPPORTED;
+  // GBLAP_MULTI_FORM=blocks: all columns in one launch as concatenated
+  // vectors (the form every count used to take beyond 32)
+  const char* form = getenv("GBLAP_MULTI_FORM");
+  if (form && !strcmp(form, "blocks")) {
+    gb_batch bt = nullptr;
+    GB_TRY(multi_batch(sys, &sys->multi, nrhs, false, &bt));
+    return batch_solve(bt, B, X, opts, iters_host, nullptr, result);
+  }
+  if (nrhs <= kIlMaxRhs) {
+    gb_batch bt = nullptr;
+    GB_TRY(multi_batch(sys, &sys->multi, nrhs, true, &bt));
+    return batch_solve(bt, B, X, opts, iters_host, nullptr, result);
+  }
+  // chunks of 32 columns and a last, shorter one, each an interleaved solve
+  // that reads the matrix once per iteration for its columns; the result
+  // aggregates the chunks as one solve's does its columns
+  gb_pcg_result acc;
+  memset(&acc, 0, sizeof acc);
+  acc.status = GB_OK;
+  const size_t n = (size_t)sys->n;
+  for (int c0 = 0; c0 < nrhs; c0 += kIlMaxRhs) {
+    const int c = std::min(kIlMaxRhs, nrhs - c0);
+    gb_batch bt = nullptr;
+    GB_TRY(multi_batch(sys, c == kIlMaxRhs ? &sys->multi : &sys->multi_tail, c, true, &bt));
+    gb_pcg_result r;
+    GB_TRY(batch_solve(bt, B + (size_t)c0 * n, X + (size_t)c0 * n, opts, iters_host ? iters_host + c0 : nullptr,
+                       nullptr, &r));
+    acc.iters = std::max(acc.iters, r.iters);
+    acc.outer = std::max(acc.outer, r.outer);
+    acc.flag = std::max(acc.flag, r.flag);
+    if (acc.status == GB_OK && r.status != GB_OK) acc.status = r.status;
+    acc.res0 = std::max(acc.res0, r.res0);
+    acc.res = std::max(acc.res, r.res);
+    acc.true_res = std::max(acc.true_res, r.true_res);
+    acc.rel_true_res = std::max(acc.rel_true_res, r.rel_true_res);
+    acc.device_ms += r.device_ms;
+  }
+  if (result) *result = acc;
+  return GB_OK;
 }

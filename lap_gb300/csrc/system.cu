@@ -135,6 +135,8 @@ static void system_free(gb_system s) {
   }
   batch_release(s->multi);
   s->multi = nullptr;
+  batch_release(s->multi_tail);
+  s->multi_tail = nullptr;
   spmv_plan_free(&s->plan);
   tri_plan_free(&s->L);
   tri_plan_free(&s->U);

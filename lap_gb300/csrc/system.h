@@ -85,7 +85,8 @@ struct gb_system_s {
   int* err = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
-  gb_batch multi = nullptr;  // gb_pcg_solve_multi's shared-matrix batch
+  gb_batch multi = nullptr;       // gb_pcg_solve_multi's shared-matrix batch (a chunk of up to 32)
+  gb_batch multi_tail = nullptr;  // ... and the last, shorter chunk when there are more than 32
   gb::LoopGraph loop[3];  // [precision]
   int loop_key[3] = {-1, -1, -1};
 };

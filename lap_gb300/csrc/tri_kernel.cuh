@@ -509,7 +509,9 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
     if (row >= t0 && row < t1) st_shared_volatile(sy + (row - t0), yv);  // the levels form has no tile rows
   }
   __syncwarp();
-  if (lane == 0) red_release_cta_add(s_done, 1);
+  // the tile-level counter is read only where rows wait on whole levels
+  if constexpr (!POLL)
+    if (lane == 0) red_release_cta_add(s_done, 1);
   if (act && (!lng || lane == 0) && !(h.flags & kRecPart)) {
     if (L.out) st_cluster(L.out + (uint32_t)(row - t0) * (uint32_t)sizeof(T), yv);  // next tile's inbox
     st_relaxed(A.y + row, yv);

@@ -116,11 +116,12 @@ def test_multi_rhs_matches_single_solves(prec):
     sysm.close()
 
 
-@pytest.mark.parametrize("nrhs", [1, 7, 32, 33])
+@pytest.mark.parametrize("nrhs", [1, 7, 32, 33, 70])
 def test_multi_rhs_layouts_match_single_solves(nrhs):
     """Up to 32 right-hand sides run on interleaved vectors (32 // nrhs rows per
-    warp step; 7 leaves idle lanes), 33 on the concatenated layout; a nonzero
-    x0 goes through the transposes in both directions."""
+    warp step; 7 leaves idle lanes); 33 and 70 as chunks of 32 and a last one
+    of 1 or 6 (the 32-column batch reused for two chunks); a nonzero x0 goes
+    through the transposes in both directions."""
     A, _ = gen.grid3d_lognormal(10, seed=1003)
     Bm = gen.multi_rhs(A.n, nrhs, seed=1006)
     X0 = np.random.default_rng(1007).uniform(-1, 1, Bm.shape)
@@ -168,6 +169,33 @@ def test_multi_rhs_split_inline_replacement(nrhs):
     assert abs(float(np.mean(its)) - float(np.mean(alone))) <= 0.02 * float(np.mean(alone))
     Xe, ie, _ = gb.solve_multi(sysm, dev(Bm), precision=2, use_graph=False, **kw)
     assert (ie == its).all() and torch.equal(Xe, X)
+    sysm.close()
+
+
+@pytest.mark.parametrize("prec", [0, 2])
+def test_multi_rhs_chunks_match_block_form(prec, monkeypatch):
+    """More than 32 right-hand sides in chunks of 32 agree with the block
+    form (all 45 columns in one launch as concatenated vectors,
+    GBLAP_MULTI_FORM=blocks) within a few iterations and 1e-8 per column;
+    the per-column counts and the aggregate are in column order; and the
+    cached chunk batches survive a solve of another count in between."""
+    A, _ = gen.grid3d_lognormal(12, seed=1009)
+    Bm = gen.multi_rhs(A.n, 45, seed=1010)
+    sysm = gb.System.from_csr(A, "line_jacobi")
+    kw = dict(tol=1e-10, maxit=20000, precision=prec)
+    X, its, r = gb.solve_multi(sysm, dev(Bm), **kw)
+    assert r["flag"] == 0 and r["iters"] == int(its.max())
+    gb.solve_multi(sysm, dev(Bm[:5]), **kw)
+    Xr, itr, _ = gb.solve_multi(sysm, dev(Bm), **kw)
+    assert (itr == its).all() and torch.equal(Xr, X)
+    monkeypatch.setenv("GBLAP_MULTI_FORM", "blocks")
+    Xb, itb, rb = gb.solve_multi(sysm, dev(Bm), **kw)
+    monkeypatch.delenv("GBLAP_MULTI_FORM")
+    assert rb["flag"] == 0
+    slack = 1 if prec == 0 else 3
+    for k in range(45):
+        assert abs(int(its[k]) - int(itb[k])) <= max(slack, int(np.ceil(0.08 * int(itb[k])))), (k, its[k], itb[k])
+        assert float(torch.linalg.norm(X[k] - Xb[k]) / torch.linalg.norm(Xb[k])) < 1e-8
     sysm.close()
 
 
