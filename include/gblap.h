@@ -224,14 +224,16 @@ typedef struct {
   int *ia, *ja;
   double *a;
   int host_parsed;       /* values outside the device's exact decimal path, parsed by strtod */
-  double read_ms;        /* host file read (gb_mm_read_csr) */
-  double h2d_ms;         /* the bytes' copy to the device */
+  double read_ms;        /* gb_mm_read_csr: the file read, with the copy to the device overlapped */
+  double h2d_ms;         /* gb_mm_parse_csr: the bytes' copy to the device (0 for a file) */
   double device_ms;      /* line split, parse, mirror, sort and CSR build */
 } gb_mm_csr;
 
 /* read_mm_file (io_utils.c:15-74) followed by coo_to_csr (io_utils.c:141-235),
- * with the same CSR bit for bit, built on the device: the host reads the file
- * and its header, the bytes are copied once, and line splitting, number
+ * with the same CSR bit for bit, built on the device: the host reads the
+ * header, reader threads read the rest in 4 MB chunks and copy each to the
+ * device while reading the next (GBLAP_MM_READ_THREADS, default 8), and
+ * line splitting, number
  * parsing (values rounded to the nearest double exactly, as strtod does),
  * symmetric mirroring and the column sort run as device kernels.  Lines
  * starting with '%' and blank lines are skipped; entries past the size line's

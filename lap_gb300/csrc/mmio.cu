@@ -10,8 +10,10 @@
 //     keeping file order -- mirrored entries at the position of the line
 //     that produced them -- as the reference's per-row sort of its
 //     row-bucketed list does for the files it is given.
-// The host reads the file and its header; one copy moves the bytes to the
-// device, where the whole conversion is integer and byte work bound by HBM:
+// The host reads the header; reader threads read the rest of the file in
+// chunks through pinned staging, each copied to the device while the next is
+// read (bytes already in host memory are copied at once).  On the device the
+// whole conversion is integer and byte work bound by HBM:
 //   1. newline count per 4 KB chunk, scan, line starts;
 //   2. one thread per line: two integers and a decimal value, rounded to the
 //      nearest double exactly (below);
@@ -26,16 +28,25 @@
 // remainder as sticky bit, s chosen so the quotient has 55-56 bits, times
 // 2^(-s+E).  Rounding is to nearest, ties to even, as strtod does.  Any other
 // value (more digits, larger exponents, inf, nan, hex) is parsed by strtod
-// on the host, for the lines that need it.
+// on the host, for the lines that need it, packed on the device and copied
+// back.
 #include <cuda_runtime.h>
 
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <algorithm>
+#include <atomic>
+#include <cerrno>
 #include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "gb_common.cuh"
@@ -384,6 +395,16 @@ __global__ void gather_lines_kernel(int k, const int* __restrict__ lines, const 
   }
 }
 
+// the bytes of those lines, packed end to end for one copy to the host
+// (one block per line; se and po hold offsets inside buf and out)
+__global__ void pack_lines_kernel(int k, const long long* __restrict__ se, const long long* __restrict__ po,
+                                  const unsigned char* __restrict__ buf, char* __restrict__ out) {
+  const int i = blockIdx.x;
+  if (i >= k) return;
+  const long long s0 = se[2 * i], len = se[2 * i + 1] - s0, o = po[i];
+  for (long long j = threadIdx.x; j < len; j += blockDim.x) out[o + j] = (char)buf[s0 + j];
+}
+
 // host-parsed values into their lines
 __global__ void patch_values_kernel(int k, const int* __restrict__ lines, const double* __restrict__ v, double* val) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -632,6 +653,121 @@ int bits_for(long long v) {  // bits to hold 0..v
   return b;
 }
 
+// Reader threads and the pinned staging they share: each thread owns two
+// chunks of staging and alternates between them, reading one while the
+// other's copy to the device is in flight.
+constexpr long long kReadChunk = 4ll << 20;
+constexpr int kReadThreadsMax = 8;
+
+int read_threads() {
+  int t = kReadThreadsMax;
+  if (const char* e = getenv("GBLAP_MM_READ_THREADS")) t = atoi(e);
+  const int hw = (int)std::thread::hardware_concurrency();
+  if (hw > 0) t = std::min(t, hw);
+  return std::max(1, std::min(t, kReadThreadsMax));
+}
+
+// Pinned staging kept for the process's lifetime (like the CUDA context it
+// belongs to): pinning the whole file, or even 64 MB, per call costs more
+// than reading it.  One reader at a time holds it.
+struct Staging {
+  std::mutex mu;
+  unsigned char* p = nullptr;
+  size_t bytes = 0;
+};
+Staging& staging() {
+  static Staging* st = new Staging();
+  return *st;
+}
+
+// Bytes [off, off + n) of the open file into device memory dst.  Chunk c
+// goes to thread c % T, which preads it into its free staging chunk and
+// copies it to the device on its own stream while reading its next chunk,
+// so the page-cache copy runs on T cores and overlaps the transfer.
+// Returns after every copy has completed.
+int read_file_to_device(int fd, long long off, long long n, unsigned char* dst) {
+  if (n <= 0) return GB_OK;
+  const long long nch = (n + kReadChunk - 1) / kReadChunk;
+  const int T = (int)std::min<long long>(nch, read_threads());
+  Staging& st = staging();
+  std::lock_guard<std::mutex> lock(st.mu);
+  const size_t need = (size_t)2 * kReadThreadsMax * kReadChunk;
+  if (st.bytes < need) {
+    if (st.p) cudaFreeHost(st.p);
+    st.p = nullptr;
+    st.bytes = 0;
+    if (cudaMallocHost(&st.p, need) != cudaSuccess) {
+      cudaGetLastError();
+      st.p = nullptr;
+      return GB_NO_MEMORY;
+    }
+    st.bytes = need;
+  }
+  int dev = 0;
+  GB_CUDA_TRY(cudaGetDevice(&dev));
+  std::atomic<int> err{GB_OK};
+  auto fail = [&](int code) {
+    int ok = GB_OK;
+    err.compare_exchange_strong(ok, code);
+  };
+  auto work = [&](int t) {
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    if (cudaSetDevice(dev) != cudaSuccess || cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      fail(GB_CUDA_ERROR);
+    } else {
+      int j = 0;
+      for (long long c = t; c < nch && err.load() == GB_OK; c += T, ++j) {
+        unsigned char* sb = st.p + (size_t)(2 * t + (j & 1)) * kReadChunk;
+        // the chunk's earlier copy out of this staging must have left it
+        if (j >= 2 && cudaEventSynchronize(ev[j & 1]) != cudaSuccess) {
+          fail(GB_CUDA_ERROR);
+          break;
+        }
+        const long long o = c * kReadChunk, m = std::min(kReadChunk, n - o);
+        long long got = 0;
+        while (got < m) {
+          const ssize_t r = pread(fd, sb + got, (size_t)(m - got), (off_t)(off + o + got));
+          if (r < 0 && errno == EINTR) continue;
+          if (r <= 0) break;
+          got += r;
+        }
+        if (got < m) {
+          fail(GB_BAD_INPUT);
+          break;
+        }
+        if (cudaMemcpyAsync(dst + o, sb, (size_t)m, cudaMemcpyHostToDevice, cs) != cudaSuccess ||
+            cudaEventRecord(ev[j & 1], cs) != cudaSuccess) {
+          fail(GB_CUDA_ERROR);
+          break;
+        }
+      }
+    }
+    if (cs && cudaStreamSynchronize(cs) != cudaSuccess) fail(GB_CUDA_ERROR);
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+    if (cs) cudaStreamDestroy(cs);
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < T; ++t) th.emplace_back(work, t);
+  work(0);
+  for (auto& x : th) x.join();
+  if (err.load() == GB_BAD_INPUT) fprintf(stderr, "libgblap: Matrix Market: short read\n");
+  return err.load();
+}
+
+// Where the bytes after the size line come from: the whole input in host
+// memory, or an open file read by read_file_to_device.
+struct MmSource {
+  const char* hb = nullptr;
+  int fd = -1;
+};
+
+int mm_csr_build(Header h, long long len, const MmSource& src, gb_mm_csr* out, double read_ms, const MmMode& mode);
+
 // The conversion from host bytes (the whole file).
 int mm_csr_from_bytes(const char* hb, long long len, gb_mm_csr* out, double read_ms, const MmMode& mode) {
   Header h;
@@ -639,6 +775,12 @@ int mm_csr_from_bytes(const char* hb, long long len, gb_mm_csr* out, double read
     fprintf(stderr, "libgblap: Matrix Market: no size line\n");
     return GB_BAD_INPUT;
   }
+  MmSource src;
+  src.hb = hb;
+  return mm_csr_build(h, len, src, out, read_ms, mode);
+}
+
+int mm_csr_build(Header h, long long len, const MmSource& src, gb_mm_csr* out, double read_ms, const MmMode& mode) {
   if (mode.adjacency) h.symmetric = true;  // io_utils.c:96
   if (h.n <= 0 || h.m <= 0 || h.nnz < 0 || h.n >= (1LL << 31) - 1 || h.m >= (1LL << 31) - 1 ||
       (h.symmetric ? 2 : 1) * h.nnz >= (1LL << 31) - 1)
@@ -666,9 +808,15 @@ int mm_csr_from_bytes(const char* hb, long long len, gb_mm_csr* out, double read
   // bytes, padded to whole 16-byte loads
   unsigned char* buf = nullptr;
   GB_TRY(D.get(&buf, (size_t)dlen + 32));
+  if (src.fd >= 0 && dlen > 0) {  // a file: read and copied in overlapped chunks, counted as the read
+    const auto t0 = std::chrono::steady_clock::now();
+    GB_TRY(read_file_to_device(src.fd, h.data_off, dlen, buf));
+    read_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
   GB_CUDA_TRY(cudaEventRecord(ev[0], s));
   GB_CUDA_TRY(cudaMemsetAsync(buf + dlen, 0, 32, s));
-  if (dlen > 0) GB_CUDA_TRY(cudaMemcpyAsync(buf, hb + h.data_off, (size_t)dlen, cudaMemcpyHostToDevice, s));
+  if (src.hb && dlen > 0)
+    GB_CUDA_TRY(cudaMemcpyAsync(buf, src.hb + h.data_off, (size_t)dlen, cudaMemcpyHostToDevice, s));
   GB_CUDA_TRY(cudaEventRecord(ev[1], s));
   // 1. lines
   const int nchunk = (int)std::max(1LL, (dlen + kChunkBytes - 1) / kChunkBytes);
@@ -723,9 +871,21 @@ int mm_csr_from_bytes(const char* hb, long long len, gb_mm_csr* out, double read
     std::vector<long long> se(2 * (size_t)nh);
     GB_CUDA_TRY(cudaMemcpyAsync(se.data(), dse, sizeof(long long) * 2 * nh, cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaStreamSynchronize(s));
+    // the lines' bytes from the device copy (a file's bytes are not kept on the host)
+    std::vector<long long> po(nh + 1, 0);
+    for (int i = 0; i < nh; ++i) po[i + 1] = po[i] + (se[2 * i + 1] - se[2 * i]);
+    long long* dpo = nullptr;
+    char* dpk = nullptr;
+    GB_TRY(D.get(&dpo, nh));
+    GB_TRY(D.get(&dpk, (size_t)po[nh]));
+    GB_CUDA_TRY(cudaMemcpyAsync(dpo, po.data(), sizeof(long long) * nh, cudaMemcpyHostToDevice, s));
+    pack_lines_kernel<<<nh, 128, 0, s>>>(nh, dse, dpo, buf, dpk);
+    std::vector<char> pk((size_t)po[nh] + 1);
+    if (po[nh] > 0) GB_CUDA_TRY(cudaMemcpyAsync(pk.data(), dpk, (size_t)po[nh], cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
     std::vector<double> vals(nh);
     for (int i = 0; i < nh; ++i) {
-      const std::string line(hb + h.data_off + se[2 * i], (size_t)(se[2 * i + 1] - se[2 * i]));
+      const std::string line(pk.data() + po[i], (size_t)(po[i + 1] - po[i]));
       long long r, c;
       double v = 0.0;
       sscanf(line.c_str(), "%lld %lld %lf", &r, &c, &v);
@@ -832,31 +992,43 @@ int mm_read_file(const char* path, gb_mm_csr* out, const MmMode& mode) {
   if (!path || !out) return GB_BAD_INPUT;
   memset(out, 0, sizeof *out);
   const auto t0 = std::chrono::steady_clock::now();
-  FILE* f = fopen(path, "rb");
-  if (!f) {
+  const int fd = open(path, O_RDONLY);
+  if (fd < 0) {
     fprintf(stderr, "libgblap: gb_mm_read_csr: cannot open %s\n", path);
     return GB_BAD_INPUT;
   }
-  fseek(f, 0, SEEK_END);
-  const long long len = ftell(f);
-  fseek(f, 0, SEEK_SET);
-  if (len <= 0) {
-    fclose(f);
-    return GB_BAD_INPUT;
+  struct FdGuard {
+    int fd;
+    ~FdGuard() { close(fd); }
+  } fg{fd};
+  struct stat sb;
+  if (fstat(fd, &sb) != 0 || sb.st_size <= 0) return GB_BAD_INPUT;
+  const long long len = (long long)sb.st_size;
+  // the banner, comments and size line, read until the size line ends
+  // inside what was read (or the file does)
+  std::vector<char> head;
+  Header h;
+  for (long long want = std::min(len, 1ll << 16);; want = std::min(len, 2 * want)) {
+    head.resize((size_t)want);
+    long long got = 0;
+    while (got < want) {
+      const ssize_t r = pread(fd, head.data() + got, (size_t)(want - got), (off_t)got);
+      if (r < 0 && errno == EINTR) continue;
+      if (r <= 0) break;
+      got += r;
+    }
+    if (got < want) return GB_BAD_INPUT;
+    const bool ok = parse_header(head.data(), want, &h);
+    if (ok && (want == len || (h.data_off <= want && head[(size_t)h.data_off - 1] == '\n'))) break;
+    if (want == len) {
+      fprintf(stderr, "libgblap: Matrix Market: no size line\n");
+      return GB_BAD_INPUT;
+    }
   }
-  char* hb = nullptr;  // pinned, so the copy to the device runs at full speed
-  if (cudaMallocHost(&hb, (size_t)len) != cudaSuccess) {
-    cudaGetLastError();
-    fclose(f);
-    return GB_NO_MEMORY;
-  }
-  const size_t got = fread(hb, 1, (size_t)len, f);
-  fclose(f);
-  const double read_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-  int rc = GB_BAD_INPUT;
-  if ((long long)got == len) rc = mm_csr_from_bytes(hb, len, out, read_ms, mode);
-  cudaFreeHost(hb);
-  return rc;
+  const double head_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  MmSource src;
+  src.fd = fd;
+  return mm_csr_build(h, len, src, out, head_ms, mode);
 }
 
 MmMode laplacian_mode(int weighted, int exact) {

@@ -78,6 +78,61 @@ def test_generated_laplacian_file(tmp_path):
     _same(p.read_bytes())
 
 
+def _same_file(tmp_path, data, name="t.mtx"):
+    """The file path (header read, chunked reader threads) against the
+    oracle on the same bytes."""
+    p = tmp_path / name
+    p.write_bytes(data)
+    ia, ja, a, info = gb.read_mm_device(str(p))
+    n, m, sym, oia, oja, oa = oracle.mm_csr(data)
+    assert (info["n"], info["m"], bool(info["symmetric"])) == (n, m, sym)
+    assert np.array_equal(ia.cpu().numpy(), oia) and np.array_equal(ja.cpu().numpy(), oja)
+    assert np.array_equal(a.cpu().numpy().view(np.int64), oa.view(np.int64))
+    return info
+
+
+@pytest.fixture(scope="module")
+def g64_file(tmp_path_factory):
+    A, _ = gen.grid3d_lognormal(64, seed=1011)
+    p = tmp_path_factory.mktemp("mm") / "g64.mtx"
+    gen.write_mm(str(p), A)
+    return A, p
+
+
+@pytest.mark.parametrize("threads", ["1", "2", "8"])
+def test_file_reader_chunks(g64_file, monkeypatch, threads):
+    """A 34 MB file (nine 4 MB chunks; with 2 threads each reuses its two
+    staging chunks) gives the same CSR with 1, 2 or 8 reader threads."""
+    monkeypatch.setenv("GBLAP_MM_READ_THREADS", threads)
+    A, p = g64_file
+    assert p.stat().st_size > 8 * (4 << 20)
+    ia, ja, a, info = gb.read_mm_device(str(p))
+    assert info["host_parsed"] == 0 and info["nnz"] == len(A.ja)
+    assert np.array_equal(ia.cpu().numpy(), A.ia) and np.array_equal(ja.cpu().numpy(), A.ja)
+    assert np.array_equal(a.cpu().numpy(), A.a)
+
+
+def test_file_reader_host_parsed_and_headers(tmp_path):
+    """From a file: lines left to strtod (their bytes come back from the
+    device copy), a comment block longer than the first header read, and a
+    file that ends on its size line."""
+    info = _same_file(tmp_path, mm_cases.general_text().encode(), "g.mtx")
+    assert info["host_parsed"] > 0
+    long_comments = "%%MatrixMarket matrix coordinate real general\n" + \
+        "".join(f"% comment line {i:06d} " + "x" * 80 + "\n" for i in range(1500)) + \
+        mm_cases.general_text(seed=9).split("\n", 1)[1]
+    assert len(long_comments) > 2 * (1 << 16)
+    _same_file(tmp_path, long_comments.encode(), "c.mtx")
+    ia, ja, a, info = gb.read_mm_device(str(_write(tmp_path / "e.mtx",
+                                                   b"%%MatrixMarket matrix coordinate real general\n3 3 0")))
+    assert info["nnz"] == 0 and ia.cpu().tolist() == [0, 0, 0, 0]
+
+
+def _write(p, data):
+    p.write_bytes(data)
+    return p
+
+
 def test_edge_cases():
     # no entries
     ia, ja, a, info = gb.read_mm_device(data=b"%%MatrixMarket matrix coordinate real general\n3 3 0\n")
