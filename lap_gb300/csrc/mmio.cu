@@ -752,7 +752,14 @@ int read_file_to_device(int fd, long long off, long long n, unsigned char* dst) 
     if (cs) cudaStreamDestroy(cs);
   };
   std::vector<std::thread> th;
-  for (int t = 1; t < T; ++t) th.emplace_back(work, t);
+  for (int t = 1; t < T; ++t) {
+    try {
+      th.emplace_back(work, t);
+    } catch (...) {  // no thread: its chunks stay unread, so the read fails as a whole
+      fail(GB_NO_MEMORY);
+      break;
+    }
+  }
   work(0);
   for (auto& x : th) x.join();
   if (err.load() == GB_BAD_INPUT) fprintf(stderr, "libgblap: Matrix Market: short read\n");
