@@ -235,8 +235,10 @@ def _edge_positions(A, ei, ej):
 
 
 def run_workload(args, local):
-    """The survey's other configurations at full size (parity cases beside the
-    headline bench line): one JSON line each with times and accuracy."""
+    """The other configurations at full size (256^2 Jacobi, Chung-Lu, the
+    kNN batch, multi-RHS, the adjoint, the Matrix Market read; parity cases
+    beside the headline bench line): one JSON line each with times and
+    accuracy."""
     import torch
 
     import lap_gb300 as gb
