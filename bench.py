@@ -13,14 +13,21 @@ Workload (one "step" = one full solve from x0 = 0):
            iterative refinement (reported beside; needs ~1.75x the iterations);
   e2e    = the same mixed solve through gb_pcg_solve_host from pinned host
            buffers (b, x0 in; x out), copies inside the timed region.
+  parity = every GPU solve against the reference's CPU PCG on the same
+           inputs at full size (IC(0) and GS_std, k = 1): its iteration count
+           and the relative distance of x from the reference's x.
+  cpu_baseline = one full FP64 IC(0)-PCG solve by the reference's algorithm
+           (the oracle's C restatement of LAP's serial path) on one host core,
+           measured, not extrapolated.
 Inputs (matrix 175 MB FP64 + 117 MB FP32 copy + factors) exceed the 129 MB L2,
 so no explicit L2 flush is done between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
---impl reference times the reference's CPU algorithm (the oracle's C
-restatement, multithreaded SpMV/dot as LAP's OpenMP backend) on this host on a
-bounded sample of iterations, scaled to the full iteration count.
+--impl reference times the reference's CPU algorithm on this host: the
+oracle's restatement of LAP's OpenMP backend (SpMV on a team of 16 threads as
+openmp_blas.c:37 fixes it, dot on all host threads, serial triangular
+solves).  Each timed step is one full solve; warm-up steps are short samples.
 """
 from __future__ import annotations
 
@@ -146,19 +153,51 @@ def make_workload(nside):
     return gen.grid3d_lognormal(nside, seed=1002)
 
 
-def cpu_baseline(A, b, full_iters, target_s=12.0, kind="serial"):
-    """The oracle (our C restatement of LAP's CPU PCG) on a bounded sample."""
+def host_info():
+    """Host cores, CPU model and OMP_NUM_THREADS of the machine the CPU legs ran on."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if model is None and os.path.exists("/proc/cpuinfo"):
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part")):
+                    model = line.split(":", 1)[1].strip()
+                    break
+    return {"nproc": os.cpu_count(), "cpu_model": model, "machine": os.uname().machine,
+            "omp_num_threads": os.environ.get("OMP_NUM_THREADS")}
+
+
+def reference_solve(A, b, prec, tol, kind="serial", max_iters_run=0):
+    """The reference's CPU PCG (the oracle: LAP's serial path restated, or its
+    OpenMP backend mirror) on the full system, from x0 = 0."""
     import oracle
 
-    probe = oracle.solve(A.n, A.ia, A.ja, A.a, b, "ichol", 1e-8, 100000, kind=kind, max_iters_run=3)
-    per_it = probe["solve_s"] / max(probe["iters"], 1)
-    m = int(max(3, min(full_iters, target_s / max(per_it, 1e-6))))
-    r = oracle.solve(A.n, A.ia, A.ja, A.a, b, "ichol", 1e-8, 100000, kind=kind, max_iters_run=m)
-    per_it = r["solve_s"] / max(r["iters"], 1)
-    return dict(value=per_it * full_iters * 1e3, unit=UNIT, cores=oracle.lib(kind).orc_num_threads(),
-                kind="port", sample=f"{r['iters']} of {full_iters} IC0-PCG iterations (FP64, CPU) on "
-                f"the full 128^3 matrix, {per_it * 1e3:.1f} ms/iteration, scaled to the full solve; "
-                f"IC0 setup {r['setup_s']:.1f} s excluded as LAP's Time line excludes it")
+    return oracle.solve(A.n, A.ia, A.ja, A.a, b, prec, tol, 20000, kind=kind, max_iters_run=max_iters_run)
+
+
+def cpu_baseline(ref):
+    """Measured time of one full serial solve (cg() only, as LAP's Time line)."""
+    return dict(value=round(ref["solve_s"] * 1e3, 1), unit=UNIT, cores=1, kind="port",
+                sample=f"one full FP64 IC0-PCG solve of the 128^3 system ({ref['iters']} iterations) by the "
+                       f"oracle's restatement of LAP's serial path on 1 host core; cg() only, as LAP's Time "
+                       f"line; IC0 setup {ref['setup_s']:.2f} s excluded",
+                host=host_info())
+
+
+def parity_entry(ref, x, r):
+    """A GPU solve against the reference's: iterations and distance of x."""
+    xr = ref["x"]
+    err = float(np.linalg.norm(x.cpu().numpy() - xr) / np.linalg.norm(xr))
+    slack = max(1, int(np.ceil(0.02 * ref["iters"])))
+    return {"iters": r["iters"], "x_rel_err_vs_reference": err, "rel_true_res": r["rel_true_res"],
+            "iters_within_2pct": abs(r["iters"] - ref["iters"]) <= slack, "x_within_1e-6": err <= 1e-6}
 
 
 def run_reference(args, world, rank):
@@ -169,28 +208,28 @@ def run_reference(args, world, rank):
 
     A, b = make_workload(args.size)
     t0 = time.time()
-    full = oracle.solve(A.n, A.ia, A.ja, A.a, b, "ichol", 1e-8, 100000, kind="omp")
-    iters = full["iters"]
-    m = max(2, min(iters, args.sample_iters))
-    times = []
-    for s in range(args.warmup + args.steps):
-        r = oracle.solve(A.n, A.ia, A.ja, A.a, b, "ichol", 1e-8, 100000, kind="omp", max_iters_run=m)
-        if s >= args.warmup:
-            times.append(r["solve_s"] / r["iters"] * iters * 1e3)
+    for _ in range(args.warmup):  # untimed: page in the matrix, start the thread team
+        reference_solve(A, b, "ichol", args.tol, kind="omp", max_iters_run=3)
+    times, iters = [], []
+    for _ in range(args.steps):  # each timed step: one full solve
+        r = reference_solve(A, b, "ichol", args.tol, kind="omp")
+        times.append(r["solve_s"] * 1e3)
+        iters.append(r["iters"])
     v = statistics.mean(times)
-    cores = oracle.lib("omp").orc_num_threads()
-    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
+    L = oracle.lib("omp")
+    spmv_t, dot_t = L.orc_spmv_threads(), L.orc_num_threads()
+    line = {"metric": METRIC, "value": round(v, 1), "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v, 1), "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD + " (reference: FP64 IC0-PCG, CPU)", "iterations": iters,
-                       "sample_iterations": m},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{m} of {iters} IC0-PCG iterations per step on the full "
-                                       f"matrix, scaled to the full solve; LAP OpenMP backend "
-                                       f"mirror (SpMV/dot on {cores} threads, serial triangular "
-                                       f"solves)"},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "wall_s": time.time() - t0}
+            "config": {"workload": WORKLOAD + " (reference: FP64 IC0-PCG, CPU)", "iterations": iters[-1],
+                       "flag": r["flag"], "steps_ms": [round(t, 1) for t in times]},
+            "cpu_baseline": {"value": round(v, 1), "unit": UNIT, "cores": max(spmv_t, dot_t), "kind": "port",
+                             "sample": f"one full solve per step ({iters[-1]} iterations, cg() only as LAP's "
+                                       f"Time line); restatement of LAP's OpenMP backend: SpMV on {spmv_t} "
+                                       f"threads (openmp_blas.c:37), dot on {dot_t}, serial triangular solves",
+                             "host": host_info()},
+            "e2e": {"value": round(v, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": round(time.time() - t0, 1)}
     print(json.dumps(line), flush=True)
 
 
@@ -455,7 +494,7 @@ def run_ours(args, world, rank, local):
         ms_mixed, r_mixed, x_mixed = timed(MIXED, args.steps)
         wall = time.time() - t0
     ms_fp64, r_fp64, x_fp64 = timed(0, max(2, args.steps // 2))
-    ms_f32k, r_f32k, _ = timed(1, 2)
+    ms_f32k, r_f32k, x_f32k = timed(1, 2)
     err_vs_fp64 = float(torch.linalg.norm(x_mixed - x_fp64) / torch.linalg.norm(x_fp64))
 
     # end to end from pinned host buffers
@@ -533,8 +572,41 @@ def run_ours(args, world, rank, local):
             "gpu_launches": launches_mixed * args.steps,
             "clocks": clk.summary(), "wall_s_timed": round(wall, 3)}
     if world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(A, b, r_fp64["iters"])
+        # the reference's CPU PCG on the same system: the measured CPU
+        # baseline, and what every GPU solve's x and iteration count are
+        # checked against
+        ref = reference_solve(A, b, "ichol", args.tol)
+        line["cpu_baseline"] = cpu_baseline(ref)
+        line["parity"] = {
+            "reference": "oracle: C restatement of LAP's serial PCG (cg.c, simple_blas.c), pinned bit for bit "
+                         "to LAP's own compiled code on the golden fixtures; same system, b, tol, x0 = 0",
+            "bar": "x within 1e-6 relative of the reference's x; iterations within +-2% (GS / IC0)",
+            "ichol": {"ref_iters": ref["iters"], "ref_flag": ref["flag"],
+                      "fp64": parity_entry(ref, x_fp64, r_fp64),
+                      "mixed": parity_entry(ref, x_mixed, r_mixed),
+                      "fp32_krylov": parity_entry(ref, x_f32k, r_f32k)}}
+        if not args.no_gs_parity:
+            line["parity"]["GS_std"] = gs_parity(A, b, db, args.tol)
     print(json.dumps(line), flush=True)
+
+
+def gs_parity(A, b, db, tol):
+    """GS_std (M = K = 1) on the headline system in the three precision modes,
+    against the reference's CPU GS_std-PCG."""
+    import lap_gb300 as gb
+
+    sg = gb.System.from_csr(A, "GS_std")
+    res = {}
+    for p in (0, 1, 2):
+        sg.solve(db, precision=p, tol=tol, maxit=20000)  # graph capture
+        res[p] = sg.solve(db, precision=p, tol=tol, maxit=20000)
+    sg.close()
+    ref = reference_solve(A, b, "GS_std", tol)
+    out = {"ref_iters": ref["iters"], "ref_flag": ref["flag"], "ref_cpu_ms_1core": round(ref["solve_s"] * 1e3, 1)}
+    for p, name in ((0, "fp64"), (2, "mixed"), (1, "fp32_krylov")):
+        x, r = res[p]
+        out[name] = dict(parity_entry(ref, x, r), ms=round(r["device_ms"], 3))
+    return out
 
 
 def main():
@@ -545,8 +617,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--size", type=int, default=128)
     ap.add_argument("--tol", type=float, default=1e-8)
-    ap.add_argument("--sample-iters", type=int, default=20)
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the CPU reference solves (baseline and parity)")
+    ap.add_argument("--no-gs-parity", action="store_true", help="skip the GS_std parity solves")
     ap.add_argument("--kernels-only", action="store_true",
                     help="only the eager per-kernel profile of each precision mode (for ncu)")
     ap.add_argument("--profile-iters", type=int, default=3)

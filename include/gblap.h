@@ -207,9 +207,11 @@ int gb_profile_iteration(gb_system sys, const double *b, double *x, int precisio
  *     capture begins.
  *   - Calls that can overlap on one device (several host threads, or
  *     unordered streams) share the scratch and race: serialise them.
- * stream: a cudaStream_t, or NULL for the legacy default stream; the call
- * returns after the result has reached *result_host.  The rounding depends on
- * n only (fixed chunking), and may differ from cuda_dot() in the last bits. */
+ * stream: a cudaStream_t, or NULL for the legacy default stream.  Every
+ * call blocks: it ends with a copy of the result into *result_host and
+ * waits for the stream, so it returns with the sum in hand.  The rounding
+ * depends on n only (fixed chunking), and may differ from cuda_dot() in the
+ * last bits. */
 int gb_dot_noalloc(int n, const double *v, const double *w, double *result_host, void *stream);
 
 /* ------------------------------------------------------------ Matrix Market on the device */

@@ -109,6 +109,23 @@ extern "C" int gb_adjoint_grad(gb_system s, const double* x, const double* g, do
   return gb_adjoint_scatter(s, x, lambda, G, edge_grad);
 }
 
+// CUDA events destroyed on every exit path of the timing helpers below.
+namespace {
+struct EventSet {
+  std::vector<cudaEvent_t> ev;
+  int create(int n) {
+    ev.assign(n, nullptr);
+    for (auto& e : ev) GB_CUDA_TRY(cudaEventCreate(&e));
+    return GB_OK;
+  }
+  cudaEvent_t operator[](int i) const { return ev[i]; }
+  ~EventSet() {
+    for (auto e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+};
+}  // namespace
+
 // ------------------------------------------------------------ autotuner
 namespace {
 std::mutex g_tune_mu;
@@ -129,12 +146,16 @@ extern "C" int gb_autotune_spmv(gb_system s, int* best_host) {
   if (best < 0) {
     const int candidates[] = {32, 16, 8, 4};
     float best_ms = 1e30f;
-    cudaEvent_t e0, e1;
-    GB_CUDA_TRY(cudaEventCreate(&e0));
-    GB_CUDA_TRY(cudaEventCreate(&e1));
+    EventSet ev;
+    GB_TRY(ev.create(2));
+    const cudaEvent_t e0 = ev[0], e1 = ev[1];
     for (int rpb : candidates) {
       SpmvPlan p;
       GB_TRY(spmv_plan_build(s->n, s->nnz, s->h_ia.data(), &p, rpb));
+      struct PlanFree {
+        SpmvPlan* p;
+        ~PlanFree() { spmv_plan_free(p); }
+      } pf{&p};
       for (int w = 0; w < 3; ++w)
         GB_TRY(spmv_axpby<double>(&p, s->n, s->ia, s->ja, s->a, 1.0, s->v64.p0, 0.0, s->v64.q, s->s));
       GB_CUDA_TRY(cudaEventRecord(e0, s->s));
@@ -145,14 +166,11 @@ extern "C" int gb_autotune_spmv(gb_system s, int* best_host) {
       GB_CUDA_TRY(cudaEventSynchronize(e1));
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e0, e1);
-      spmv_plan_free(&p);
       if (ms < best_ms) {
         best_ms = ms;
         best = rpb;
       }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune_cache[key] = best;
   }
@@ -202,9 +220,10 @@ extern "C" int gb_profile_iteration(gb_system s, const double* b, double* x, int
   }
   GB_CUDA_TRY(cudaStreamSynchronize(s->s));
   ProfHook hook;
-  cudaEvent_t start;
-  GB_CUDA_TRY(cudaEventCreate(&start));
-  for (int i = 0; i < ProfHook::kMax; ++i) GB_CUDA_TRY(cudaEventCreate(&hook.ev[i]));
+  EventSet ev;
+  GB_TRY(ev.create(ProfHook::kMax + 1));
+  const cudaEvent_t start = ev[0];
+  for (int i = 0; i < ProfHook::kMax; ++i) hook.ev[i] = ev[i + 1];
   std::vector<double> acc(ProfHook::kMax, 0.0);
   int nk = 0;
   int rc = GB_OK;
@@ -224,8 +243,6 @@ extern "C" int gb_profile_iteration(gb_system s, const double* b, double* x, int
       acc[k] += ms;
     }
   }
-  cudaEventDestroy(start);
-  for (int i = 0; i < ProfHook::kMax; ++i) cudaEventDestroy(hook.ev[i]);
   if (rc != GB_OK) return rc;
   std::string names;
   const int outk = std::min(nk, max_kernels);

@@ -23,6 +23,8 @@
 //   * there is one scratch array per device and process: calls that can
 //     overlap on a device (several host threads, or unordered streams) race
 //     on it and return wrong sums.  Serialise them;
+//   * every call blocks the calling thread: it copies the 8-byte result into
+//     the caller's host variable and waits for the stream;
 //   * the completion ticket must be zero when the kernel starts: every call
 //     clears it on its stream before the launch, and the last block clears it
 //     again on the way out.  Partials and the result slot are written before
@@ -78,6 +80,7 @@ __global__ void __launch_bounds__(kRedThreads)
   }
   __syncthreads();
   if (!last) return;
+  __threadfence();  // acquire side: the other blocks' partials, read by every thread below
   // the last block: partials in chunk order, fixed per-thread striding
   double t[1] = {0.0};
   for (int c = threadIdx.x; c < nchunks; c += blockDim.x) t[0] += ld_relaxed(part + c);

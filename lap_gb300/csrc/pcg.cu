@@ -57,6 +57,7 @@ __device__ __forceinline__ bool reduce_last(double (&v)[NV], double* part, int n
   }
   __syncthreads();
   if (!last) return false;
+  __threadfence();  // acquire side: the other blocks' partials, read by every thread below
   double t[NV];
 #pragma unroll
   for (int k = 0; k < NV; ++k) {

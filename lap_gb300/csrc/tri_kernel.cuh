@@ -33,9 +33,11 @@
 //
 // OP contract (right-hand side and epilogue of each solved row):
 //   void begin();  bool active();  void inactive_end()   (block 0, !active)
-//   Pre pre(int row)                loads of the rhs (issued early)
+//   Pre pre(int row)                loads of the rhs (issued early, up to one
+//                                   record ahead: they may read only data
+//                                   written before the launch)
 //   T rhs(int row, const Pre&)      rhs value (may store updated vectors)
-//   DPre dpre(int row)              loads for the epilogue
+//   DPre dpre(int row)              loads for the epilogue (same rule)
 //   void done(int row, T y, const DPre&)
 //   void prefetch(int r0, int r1, int part)   producer lane `part` (of
 //        kTriProdLanes), once per tile: L2 prefetch of its share of the
@@ -55,10 +57,22 @@ namespace gb {
 // Consumer warps per CTA.  FP64 solves use 8: GB300 issues one FP64 lane op
 // per two cycles per SM sub-partition, so more warps only queue their FP64
 // work in front of the dependency chain.  FP32 solves have no such limit and
-// use 16, which keeps more records' loads in flight.
+// use 15: with the producer that is 16 warps, 4 per SM sub-partition, which
+// leaves 128 registers a thread (a 17-warp block is capped at 96, and the
+// record code then spills around its waits).
+#ifndef GB_TRI_CONSUMERS32
+#define GB_TRI_CONSUMERS32 15
+#endif
+// 1: a consumer warp issues the right-hand-side loads of its next record
+// (pre / dpre) as soon as that record has landed in the ring, while it
+// solves the current one, so a record's L2 round trip for its rhs is off
+// the warp's serial path.
+#ifndef GB_TRI_RHS_AHEAD
+#define GB_TRI_RHS_AHEAD 1
+#endif
 template <typename T>
 struct TriCons {
-  static constexpr int n = sizeof(T) == 8 ? 8 : 16;
+  static constexpr int n = sizeof(T) == 8 ? 8 : GB_TRI_CONSUMERS32;
   static constexpr int threads = (n + 1) * 32;  // + one producer warp
 };
 constexpr int kTriSlots = 40;                          // ring depth (records in flight)
@@ -328,10 +342,26 @@ struct op_polls_values : std::false_type {};
 template <typename OP>
 struct op_polls_values<OP, std::void_t<decltype(OP::kPollValues)>> : std::bool_constant<OP::kPollValues> {};
 
+// The row a lane solves in a staged record (-1: idle lane).
+__device__ __forceinline__ int record_row(const unsigned char* rec, int lane) {
+  const RecHdr* h = reinterpret_cast<const RecHdr*>(rec);
+  const bool lng = (h->flags & kRecLong) != 0;
+  const int* rows = reinterpret_cast<const int*>(rec + sizeof(RecHdr));
+  return (lng || lane < h->nrows) ? rows[lng ? 0 : lane] : -1;
+}
+
+// Right-hand-side loads of a record issued ahead of it (have: they were).
+template <typename OP>
+struct RhsAhead {
+  typename OP::Pre pr;
+  typename OP::DPre dp;
+  bool have = false;
+};
+
 template <typename T, bool EXACT, bool POLL, typename OP>
 __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy, int t0, int t1,
                                              const unsigned char* rec, int lane, int* s_done,
-                                             const TriLink<T>& L) {
+                                             const TriLink<T>& L, const RhsAhead<OP>& ahead) {
   const RecHdr h = *reinterpret_cast<const RecHdr*>(rec);
   const int R4 = (h.nrows + 3) & ~3;
   const int* rows = reinterpret_cast<const int*>(rec + sizeof(RecHdr));
@@ -343,8 +373,13 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
   typename OP::Pre pr;
   typename OP::DPre dp;
   if (act) {
-    pr = op.pre(row);
-    dp = op.dpre(row);
+    if (ahead.have) {
+      pr = ahead.pr;
+      dp = ahead.dp;
+    } else {
+      pr = op.pre(row);
+      dp = op.dpre(row);
+    }
   }
   const int* cols = reinterpret_cast<const int*>(dinv + R4);
   const T* vals = reinterpret_cast<const T*>(cols + (size_t)h.len * R4);
@@ -680,11 +715,36 @@ __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArg
         }
         __syncwarp();
       } else {
+        RhsAhead<OP> next;  // loads issued for this warp's next record
         for (int q = wid; q < nrec; q += kTriConsumers) {
           const unsigned u = base + q;
           const int slot = u % kTriSlots;
           if (!failed && !mbar_wait(&full_bar[slot], (u / kTriSlots) & 1u, A.err)) failed = true;
-          if (!failed) solve_record<T, EXACT, POLL>(A, op, sy, t0, t1, ring + slot * kTriSlotBytes, lane, &s_done, link);
+          const RhsAhead<OP> cur = next;
+          next.have = false;
+#if GB_TRI_RHS_AHEAD
+          // The next record of this warp, if it has landed: issue its
+          // right-hand-side loads now, so they are in flight while this
+          // record waits.  s_last_u[slot] == un means the producer has
+          // issued record un into that slot (so the slot's previous record
+          // was consumed and the parity test below refers to record un);
+          // the barrier's phase then says whether it has landed.  Lanes
+          // decide independently; a lane that sees no record loads later.
+          const int qn = q + kTriConsumers;
+          if (!failed && qn < nrec) {
+            const unsigned un = base + qn;
+            const int sn = un % kTriSlots;
+            if (*(const volatile unsigned*)&s_last_u[sn] == un && mbar_try_wait(&full_bar[sn], (un / kTriSlots) & 1u)) {
+              const int rn = record_row(ring + sn * kTriSlotBytes, lane);
+              if (rn >= 0) {
+                next.pr = op.pre(rn);
+                next.dp = op.dpre(rn);
+              }
+              next.have = true;
+            }
+          }
+#endif
+          if (!failed) solve_record<T, EXACT, POLL>(A, op, sy, t0, t1, ring + slot * kTriSlotBytes, lane, &s_done, link, cur);
           __syncwarp();
           // after a failure the slot is not released: its copy may still be in
           // flight, and the producer must not aim another copy at it

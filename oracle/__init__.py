@@ -46,6 +46,7 @@ def _bind(lib: C.CDLL) -> C.CDLL:
                                   _dp, C.POINTER(C.c_double), C.c_int,
                                   C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.orc_num_threads.restype = C.c_int
+    lib.orc_spmv_threads.restype = C.c_int
     lib.orc_prec_apply_csr.argtypes = [C.c_int, C.c_int, _ip, _ip, _dp, C.c_char_p, C.c_int,
                                        C.c_int, _dp, _dp]
     return lib

@@ -25,9 +25,22 @@ static double wall_s(void) {
   return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
 }
 
+/* LAP's OpenMP backend runs its SpMV on a team of exactly 16 threads
+ * (openmp_blas.c:37, `omp parallel num_threads(16)`) and its dot product on
+ * the default team (openmp_blas.c:171); the mirror does the same. */
+#define ORC_SPMV_THREADS 16
+
 int orc_num_threads(void) {
 #ifdef ORC_OMP
   return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+int orc_spmv_threads(void) {
+#ifdef ORC_OMP
+  return ORC_SPMV_THREADS;
 #else
   return 1;
 #endif
@@ -81,7 +94,7 @@ void orc_csr_matvec(int n, int nnz, const int *ia, const int *ja, const double *
   (void)nnz;
   const double alpha = *alpha_p, beta = *beta_p;
 #ifdef ORC_OMP
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for num_threads(ORC_SPMV_THREADS) schedule(static)
 #endif
   for (int i = 0; i < n; ++i) {
     double acc = y[i] * beta;

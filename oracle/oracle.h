@@ -125,6 +125,7 @@ int    orc_prec_apply_csr(int n, int nnz, const int *ia, const int *ja, const do
 
 /* Number of OpenMP threads the multicore mirror uses (1 without OpenMP). */
 int    orc_num_threads(void);
+int    orc_spmv_threads(void);
 
 #ifdef __cplusplus
 }

@@ -7,6 +7,9 @@ initialised the library and its allocating paths.  Reductions are compared at
 1e-14 relative, as the other dot tests are.
 """
 import ctypes as C
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -53,3 +56,35 @@ def test_noalloc_dot_empty_and_rejections(capfd):
     assert "exceeds the static scratch limit" in capfd.readouterr().err
     # the scratch is still usable afterwards
     assert _noalloc(16, v, v) == (GB_OK, 16.0)
+
+
+_NO_GROWTH_CHILD = r"""
+import ctypes as C, sys
+import torch
+sys.path.insert(0, sys.argv[1])
+import lap_gb300 as gb
+L = gb.lib()
+n = 3_000_001
+v = torch.ones(n, dtype=torch.float64, device="cuda")
+out = C.c_double()
+torch.cuda.synchronize()
+assert L.gb_dot_noalloc(n, gb.ptr(v), gb.ptr(v), C.byref(out), None) == 0  # first call: set-up
+free0, _ = torch.cuda.mem_get_info()
+for _ in range(50):
+    assert L.gb_dot_noalloc(n, gb.ptr(v), gb.ptr(v), C.byref(out), None) == 0
+    assert out.value == float(n)
+torch.cuda.synchronize()
+free1, _ = torch.cuda.mem_get_info()
+print("free-before", free0, "free-after", free1)
+assert free1 == free0, (free0, free1)
+"""
+
+
+def test_noalloc_dot_takes_no_device_memory():
+    """The property the entry point exists for, in a fresh process: after the
+    first call (which only looks the scratch array up), fifty more calls
+    leave the device's free memory exactly where it was."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _NO_GROWTH_CHILD, root], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
