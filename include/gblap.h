@@ -62,6 +62,34 @@ int gb_system_destroy(gb_system sys);
 /* Re-reads the matrix values (same pattern) and refactors / refreshes the
  * preconditioner and the FP32 copies. */
 int gb_system_update_values(gb_system sys);
+/* Re-reads only the matrix values (same pattern) into the system's derived
+ * arrays: the FP32 copy, the diagonal and its reciprocal.  The
+ * preconditioner's values are left as they are. */
+int gb_system_refresh_matrix(gb_system sys);
+/* Loads the preconditioner's values from caller-owned device arrays laid
+ * out as LAP's pdata holds them (common.h:29-50), instead of deriving them
+ * from A -- what LAP's cg() applies through prec_function (prec.c:6-45):
+ *   line_jacobi                d_r = 1/diag (line_jacobi.c:3-7);
+ *   it_jacobi, GS_it, GS_it2   strict L (lia, lja, la, lnnz) and U, and d_r
+ *                              (it_jacobi.c:4-33, GS.c:45-159);
+ *   GS_std                     L with its diagonal last in each row and U
+ *                              with it first, as cg_driver2.c:95-144 builds
+ *                              them (GS.c:5-42);
+ *   ichol                      ichol_vals: the IC(0) factor on A's pattern
+ *                              with L in the lower triangle, as
+ *                              initialize_ichol leaves it (cuda_blas.cu:490-561).
+ * Unused arguments may be NULL.  L / U layouts must be the ones LAP's driver
+ * derives from this system's A (checked by pattern fingerprint; GB_BAD_INPUT
+ * otherwise). */
+int gb_system_set_prec_values(gb_system sys, const int *lia, const int *lja, const double *la, int lnnz,
+                              const int *uia, const int *uja, const double *ua, int unnz,
+                              const double *d_r, const double *ichol_vals);
+/* Fingerprint of a device CSR pattern (ia [n+1], ja [nnz]): a 64-bit sum of
+ * mixed (position, value) pairs, order-independent.  Caches keyed by array
+ * addresses compare it to notice new contents behind an old address.
+ * Synchronises the system's stream. */
+int gb_system_pattern_hash(gb_system sys, int n, int nnz, const int *ia, const int *ja,
+                           unsigned long long *out);
 /* Levels of the lower / upper sync-free schedules and SpMV tiles (diagnostics). */
 int gb_system_info(gb_system sys, int *lower_levels, int *upper_levels, int *spmv_tiles);
 

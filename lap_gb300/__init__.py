@@ -87,6 +87,9 @@ def _proto(L: C.CDLL) -> None:
         "gb_system_create": (i, [i, i, vp, vp, vp, C.c_char_p, i, i, C.POINTER(vp)]),
         "gb_system_destroy": (i, [vp]),
         "gb_system_update_values": (i, [vp]),
+        "gb_system_refresh_matrix": (i, [vp]),
+        "gb_system_set_prec_values": (i, [vp, vp, vp, vp, i, vp, vp, vp, i, vp, vp]),
+        "gb_system_pattern_hash": (i, [vp, i, i, vp, vp, C.POINTER(C.c_ulonglong)]),
         "gb_system_info": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
         "gb_pcg_opts_default": (None, [C.POINTER(PcgOpts)]),
         "gb_pcg_solve": (i, [vp, vp, vp, C.POINTER(PcgOpts), vp, i, C.POINTER(PcgResult)]),
@@ -125,6 +128,8 @@ def _proto(L: C.CDLL) -> None:
         "initialize_handles": (None, []),
         "initialize_ichol": (None, [i, i, vp, vp, vp]),
         "initialize_and_analyze_L_and_U_solve": (None, [i, i, vp, vp, vp, i, vp, vp, vp]),
+        "initialize_spmv_buffer": (None, [i, i, vp, vp, vp, vp, vp, C.POINTER(d), C.POINTER(d)]),
+        "initialize_L_and_U_descriptors": (None, [i, i, vp, vp, vp, i, vp, vp, vp]),
         "cuda_ichol": (None, [vp, vp, vp, i, C.POINTER(PData), vp, vp]),
         "mallocForDevice": (vp, [vp, i, i]),
         "memcpyDevice": (None, [vp, vp, i, i, C.c_char_p]),

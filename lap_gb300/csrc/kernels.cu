@@ -57,13 +57,14 @@ static int ew_grid(long long n) {
 int spmv_plan_build(int n, int nnz, const int* ia, SpmvPlan* plan, int rpb) {
   (void)nnz;
   rpb = std::max(1, std::min(rpb, kBundleRows));
+  const int cap = GB_SPMV_STAGE_A ? kBundleNnz / 2 : kBundleNnz;  // entries a bundle stages
   std::vector<int> b;
   b.reserve(n / rpb + 2);
   b.push_back(0);
   int r = 0, longs = 0;
   while (r < n) {
     const int len0 = ia[r + 1] - ia[r];
-    if (len0 > kBundleNnz) {
+    if (len0 > cap) {
       ++r;
       ++longs;
       b.push_back(r);
@@ -73,7 +74,7 @@ int spmv_plan_build(int n, int nnz, const int* ia, SpmvPlan* plan, int rpb) {
     long long nz = 0;
     while (r < n && r - start < rpb) {
       const int len = ia[r + 1] - ia[r];
-      if (nz + len > kBundleNnz) break;
+      if (nz + len > cap) break;
       nz += len;
       ++r;
     }
@@ -236,6 +237,40 @@ int cast_f64_to_f32(int n, const double* src, float* dst, cudaStream_t s) { GB_E
 int cast_f32_to_f64(int n, const float* src, double* dst, cudaStream_t s) { GB_EW_LAUNCH(cast32to64, n, src, dst); }
 int gather_values(int n, const int* map, const double* src, double* dst, float* dst32, cudaStream_t s) {
   GB_EW_LAUNCH(gather_kernel, n, map, src, dst, dst32);
+}
+
+// ------------------------------------------------------------ pattern fingerprint
+__global__ void __launch_bounds__(kRedThreads)
+    pattern_hash_kernel(int n, int nnz, const int* __restrict__ ia, const int* __restrict__ ja,
+                        unsigned long long* out) {
+  unsigned long long h = 0ull;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i <= n; i += stride)
+    h += pattern_elem(1ull, i, __ldg(ia + i));
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nnz; k += stride)
+    h += pattern_elem(2ull, k, __ldg(ja + k));
+  for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, h);
+}
+
+unsigned long long pattern_hash_host(int n, int nnz, const int* ia, const int* ja) {
+  unsigned long long h = 0ull;
+  for (long long i = 0; i <= n; ++i) h += pattern_elem(1ull, i, ia[i]);
+  for (long long k = 0; k < nnz; ++k) h += pattern_elem(2ull, k, ja[k]);
+  return h;
+}
+
+int pattern_hash(int n, int nnz, const int* ia, const int* ja, unsigned long long* dev_out, cudaStream_t s,
+                 unsigned long long* out) {
+  if (n < 0 || nnz < 0 || !ia || (nnz > 0 && !ja) || !dev_out || !out) return GB_BAD_INPUT;
+  GB_CUDA_TRY(cudaMemsetAsync(dev_out, 0, sizeof(unsigned long long), s));
+  const long long work = (long long)n + 1 + nnz;
+  const int grid = (int)std::max(1LL, std::min<long long>((work + kRedThreads - 1) / kRedThreads, reduction_grid()));
+  pattern_hash_kernel<<<grid, kRedThreads, 0, s>>>(n, nnz, ia, ja, dev_out);
+  GB_CUDA_TRY(cudaGetLastError());
+  GB_CUDA_TRY(cudaMemcpyAsync(out, dev_out, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  return GB_OK;
 }
 
 }  // namespace gb

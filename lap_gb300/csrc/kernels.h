@@ -45,4 +45,23 @@ int gather_values(int n, const int* map, const double* src, double* dst, float* 
 
 int reduction_grid();
 
+// Fingerprint of a CSR pattern (ia [n+1], ja [nnz]): the sum modulo 2^64 of
+// a 64-bit mix of every (array, position, value), so it does not depend on
+// summation order and the device and host versions agree.  Caches keyed by
+// array addresses compare it on every call, so new contents behind an old
+// address are noticed.
+__host__ __device__ inline unsigned long long pattern_mix(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__host__ __device__ inline unsigned long long pattern_elem(unsigned long long array, long long pos, int v) {
+  return pattern_mix(pattern_mix(array * 0xD6E8FEB86659FD93ull + (unsigned long long)pos) ^ (unsigned)v);
+}
+unsigned long long pattern_hash_host(int n, int nnz, const int* ia, const int* ja);
+// Device arrays; dev_out is 8 bytes of device scratch.  Synchronises s.
+int pattern_hash(int n, int nnz, const int* ia, const int* ja, unsigned long long* dev_out, cudaStream_t s,
+                 unsigned long long* out);
+
 }  // namespace gb

@@ -11,7 +11,10 @@
 // (cuda_blas.cu:10-25).  Here the analyses (level schedules) are cached per
 // factor, keyed by its row-pointer address and sizes, so several matrices
 // can be live at once; initialize_* functions build them eagerly and the
-// solves build a missing one on first use.
+// solves build a missing one on first use.  Every use recomputes the
+// pattern's fingerprint (pattern_hash, one pass over ia and ja) and rebuilds
+// the analysis when it changed: a factor freed and reallocated at the same
+// address with another pattern never runs a stale schedule.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -31,6 +34,7 @@ using namespace gb;
 namespace {
 
 struct Scratch {
+  unsigned long long* hash = nullptr;
   double* part = nullptr;
   unsigned* ticket = nullptr;
   double* out = nullptr;
@@ -42,28 +46,40 @@ struct Scratch {
 
 struct TriEntry {
   TriPlan plan;
+  unsigned long long hash = 0;
+  ~TriEntry() { tri_plan_free(&plan); }
 };
 
 struct IcEntry {
   int n = 0, nnz = 0;
+  unsigned long long hash = 0;
   TriPlan lower, upper;
   int* dpos = nullptr;
   int* tpos = nullptr;
   int* done = nullptr;
   unsigned* ticket = nullptr;
   int* zpiv = nullptr;
+  ~IcEntry() {
+    tri_plan_free(&lower);
+    tri_plan_free(&upper);
+    for (void* p : {(void*)dpos, (void*)tpos, (void*)done, (void*)ticket, (void*)zpiv})
+      if (p) cudaFree(p);
+  }
 };
 
 std::mutex g_mu;
 Scratch g_s;
-std::map<std::tuple<const void*, int, int, int>, std::unique_ptr<TriEntry>> g_tri;  // (ptr, n, nnz, lower)
-std::map<std::tuple<const void*, int, int>, std::unique_ptr<IcEntry>> g_ic;
+// heap-held and never destroyed: no cudaFree runs during static destruction
+// at exit, after the CUDA runtime may have shut down
+auto& g_tri = *new std::map<std::tuple<const void*, int, int, int>, std::unique_ptr<TriEntry>>;  // (ptr, n, nnz, lower)
+auto& g_ic = *new std::map<std::tuple<const void*, int, int>, std::unique_ptr<IcEntry>>;
 
 constexpr cudaStream_t kStream = 0;  // legacy default stream, as LAP's handles
 
 int ensure_scratch() {
   if (g_s.part) return GB_OK;
   g_s.part_len = reduction_grid() + 8;
+  GB_CUDA_TRY(cudaMalloc(&g_s.hash, sizeof(unsigned long long)));
   GB_CUDA_TRY(cudaMalloc(&g_s.part, sizeof(double) * g_s.part_len));
   GB_CUDA_TRY(cudaMalloc(&g_s.ticket, sizeof(unsigned) * 4));
   GB_CUDA_TRY(cudaMemset(g_s.ticket, 0, sizeof(unsigned) * 4));
@@ -99,16 +115,22 @@ int copy_structure(int n, int nnz, const int* ia, const int* ja, std::vector<int
 // Level schedule of a factor with its diagonal embedded (LAP GPU convention).
 int get_tri(int n, int nnz, const int* ia, const int* ja, bool lower, TriEntry** out) {
   auto key = std::make_tuple((const void*)ia, n, nnz, lower ? 1 : 0);
+  unsigned long long h = 0;
+  GB_TRY(pattern_hash(n, nnz, ia, ja, g_s.hash, kStream, &h));
   auto it = g_tri.find(key);
   if (it != g_tri.end()) {
-    *out = it->second.get();
-    return GB_OK;
+    if (it->second->hash == h) {
+      *out = it->second.get();
+      return GB_OK;
+    }
+    g_tri.erase(it);  // new pattern behind the same address
   }
   std::vector<int> hia, hja;
   GB_TRY(copy_structure(n, nnz, ia, ja, &hia, &hja));
   TriDeps d;
   GB_TRY(deps_embedded(n, hia.data(), hja.data(), lower, &d));
   auto e = std::make_unique<TriEntry>();
+  e->hash = h;
   GB_TRY(tri_plan_build(d, &e->plan));
   *out = e.get();
   g_tri[key] = std::move(e);
@@ -117,10 +139,15 @@ int get_tri(int n, int nnz, const int* ia, const int* ja, bool lower, TriEntry**
 
 int get_ic(int n, int nnz, const int* ia, const int* ja, IcEntry** out) {
   auto key = std::make_tuple((const void*)ia, n, nnz);
+  unsigned long long h = 0;
+  GB_TRY(pattern_hash(n, nnz, ia, ja, g_s.hash, kStream, &h));
   auto it = g_ic.find(key);
   if (it != g_ic.end()) {
-    *out = it->second.get();
-    return GB_OK;
+    if (it->second->hash == h) {
+      *out = it->second.get();
+      return GB_OK;
+    }
+    g_ic.erase(it);  // new pattern behind the same address
   }
   std::vector<int> hia, hja, tpos, dpos(n, -1);
   GB_TRY(copy_structure(n, nnz, ia, ja, &hia, &hja));
@@ -136,6 +163,7 @@ int get_ic(int n, int nnz, const int* ia, const int* ja, IcEntry** out) {
   auto e = std::make_unique<IcEntry>();
   e->n = n;
   e->nnz = nnz;
+  e->hash = h;
   GB_TRY(tri_plan_build(dl, &e->lower));
   GB_TRY(tri_plan_build(du, &e->upper));
   GB_CUDA_TRY(cudaMalloc(&e->dpos, sizeof(int) * n));

@@ -5,8 +5,12 @@
 // cg() keeps the reference's signature, stopping rule, flag values and
 // residual history, but runs the device-resident engine (gb_pcg_solve): no
 // host synchronisation per iteration.  The engine object for a matrix is
-// cached, so repeated cg() calls on the same (ia, ja, a, preconditioner)
-// reuse its analysis and factorization.
+// cached by (ia, ja, a, sizes, preconditioner) and revalidated on every call
+// by the fingerprint of (ia, ja), so its analysis (SpMV tiling, level
+// schedules) is reused while the pattern is the same and rebuilt when new
+// contents sit behind the same addresses.  Values are never taken from the
+// cache: each call re-reads A's values and applies the preconditioner data
+// pdata holds -- d_r, la / ua, ichol_vals -- as LAP's prec_function does.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -32,8 +36,30 @@ struct SysKey {
   }
 };
 
+struct SysEntry {
+  gb_system sys = nullptr;
+  unsigned long long pattern = 0;
+};
+
 std::mutex g_sys_mu;
-std::map<SysKey, gb_system> g_systems;
+auto& g_systems = *new std::map<SysKey, SysEntry>;  // never destroyed: no CUDA calls at exit
+
+// The preconditioner values LAP's cg() would apply: pdata's arrays where the
+// preconditioner reads them, else (arrays not set) derived from A.
+int load_prec_data(gb_system sys, const pdata* p) {
+  const int prec = gb_prec_from_name(p->prec_op);
+  const bool have = prec == GB_PREC_NONE ||
+                    (prec == GB_PREC_LINE_JACOBI && p->d_r) ||
+                    (prec == GB_PREC_ICHOL && p->ichol_vals) ||
+                    (prec == GB_PREC_GS_STD && p->lia && p->la && p->uia && p->ua) ||
+                    ((prec == GB_PREC_IT_JACOBI || prec == GB_PREC_GS_IT || prec == GB_PREC_GS_IT2) &&
+                     p->lia && p->la && p->uia && p->ua && p->d_r);
+  if (!have) return gb_system_update_values(sys);
+  const int rc = gb_system_refresh_matrix(sys);
+  if (rc != GB_OK) return rc;
+  return gb_system_set_prec_values(sys, p->lia, p->lja, p->la, p->lnnz, p->uia, p->uja, p->ua, p->unnz,
+                                   p->d_r, p->ichol_vals);
+}
 
 bool verbose() {
   const char* v = getenv("GBLAP_VERBOSE");
@@ -59,15 +85,32 @@ extern "C" void cg(int n, double nnz, int* ia, int* ja, double* a, double* x, do
     SysKey key{ia, ja, a, n, innz, prec_data->m, prec_data->k, prec_data->prec_op};
     auto f = g_systems.find(key);
     if (f != g_systems.end()) {
-      sys = f->second;
-    } else {
-      const int rc = gb_system_create(n, innz, ia, ja, a, prec_data->prec_op, prec_data->m,
-                                      prec_data->k, &sys);
+      unsigned long long h = 0;
+      const int rc = gb_system_pattern_hash(f->second.sys, n, innz, ia, ja, &h);
+      if (rc == GB_OK && h == f->second.pattern) {
+        sys = f->second.sys;
+      } else {  // another pattern behind the same addresses: rebuild
+        gb_system_destroy(f->second.sys);
+        g_systems.erase(f);
+      }
+    }
+    if (!sys) {
+      int rc = gb_system_create(n, innz, ia, ja, a, prec_data->prec_op, prec_data->m, prec_data->k, &sys);
+      SysEntry e;
+      e.sys = sys;
+      if (rc == GB_OK) rc = gb_system_pattern_hash(sys, n, innz, ia, ja, &e.pattern);
       if (rc != GB_OK) {
+        if (sys) gb_system_destroy(sys);
         fprintf(stderr, "libgblap: cg: setup failed: %s\n", gb_status_str(rc));
         return;
       }
-      g_systems[key] = sys;
+      g_systems[key] = e;
+    }
+    const int rc = load_prec_data(sys, prec_data);
+    if (rc != GB_OK) {
+      fprintf(stderr, "libgblap: cg: preconditioner data (pdata) for '%s' does not match A: %s\n",
+              prec_data->prec_op, gb_status_str(rc));
+      return;
     }
   }
   gb_pcg_opts o;

@@ -146,17 +146,22 @@ __global__ void __launch_bounds__(kThreads)
     T beta;
     bool first;
     double pq;
+    T wi, po, qo;  // loaded with the row bounds (prefetch)
+    __device__ void prefetch(int i) {
+      wi = w[i];
+      po = first ? T(0) : p[i];
+      qo = first ? T(0) : q[i];
+    }
     __device__ T init(int) const { return T(0); }
     __device__ void store(int i, T s) {
-      const T wi = w[i];
-      const T pi = first ? wi : fma_rn(beta, p[i], wi);
-      const T qi = first ? s : fma_rn(beta, q[i], s);
+      const T pi = first ? wi : fma_rn(beta, po, wi);
+      const T qi = first ? s : fma_rn(beta, qo, s);
       p[i] = pi;
       q[i] = qi;
       pq += (double)pi * (double)qi;
       if (tf) tf[i] = sentinel<T>();
     }
-  } ep{w, p, q, tfill, beta, first, 0.0};
+  } ep{w, p, q, tfill, beta, first, 0.0, T(0), T(0), T(0)};
   const int wid = threadIdx.x >> 5;
   for (int bb = blockIdx.x * (kThreads / 32) + wid; bb < nb; bb += gridDim.x * (kThreads / 32))
     spmv_bundle<T, false>(bb, n, bundles, ia, ja, a, T(1), xf, ep, stage[wid]);
@@ -370,17 +375,23 @@ __global__ void __launch_bounds__(kThreads)
     double beta;
     bool first;
     double pq;
+    float wi;
+    double po, qo;  // loaded with the row bounds (prefetch)
+    __device__ void prefetch(int i) {
+      wi = w[i];
+      po = first ? 0.0 : p[i];
+      qo = first ? 0.0 : q[i];
+    }
     __device__ float init(int) const { return 0.0f; }
     __device__ void store(int i, float s) {
-      const double wi = (double)w[i];
-      const double pi = first ? wi : fma_rn(beta, p[i], wi);
-      const double qi = first ? (double)s : fma_rn(beta, q[i], (double)s);
+      const double pi = first ? (double)wi : fma_rn(beta, po, (double)wi);
+      const double qi = first ? (double)s : fma_rn(beta, qo, (double)s);
       p[i] = pi;
       q[i] = qi;
       pq = fma_rn(pi, qi, pq);
       if (tf) tf[i] = sentinel<float>();
     }
-  } ep{w, p, q, tfill, beta, first, 0.0};
+  } ep{w, p, q, tfill, beta, first, 0.0, 0.0f, 0.0, 0.0};
   const int wid = threadIdx.x >> 5;
   for (int bb = blockIdx.x * (kThreads / 32) + wid; bb < nb; bb += gridDim.x * (kThreads / 32))
     spmv_bundle<float, false>(bb, n, bundles, ia, ja, a, 1.0f, xf, ep, stage[wid]);

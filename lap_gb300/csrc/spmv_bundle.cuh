@@ -35,12 +35,35 @@ __device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fm
 // Epilogue contract:
 //   T init(int row)           -> starting value of the row sum (beta*y or 0)
 //   void store(int row, T v)  -> consume the finished row value
+//   void prefetch(int row)    -> optional: issue the loads store() will need
+//                                (called at the start of the row's bundle)
 // X contract:
 //   T operator()(int col)     -> x value at col
-//
+template <typename EP>
+__device__ __forceinline__ auto ep_prefetch(EP& ep, int r, int) -> decltype(ep.prefetch(r), void()) {
+  ep.prefetch(r);
+}
+template <typename EP>
+__device__ __forceinline__ void ep_prefetch(EP&, int, long) {}
+
+// Values of a row held in registers from the start of its bundle (FMA
+// form): a stencil row's whole dependency list is in flight at once.
+constexpr int kSpmvHeld = 8;
+// 1: the FMA form stages the matrix values beside the gathered x (coalesced
+// loads; the row sums then read shared memory only), in bundles of half the
+// entries so the staging takes the same shared memory.
+#ifndef GB_SPMV_STAGE_A
+#define GB_SPMV_STAGE_A 0
+#endif
+
 // bundles == nullptr selects the plan-free layout: bundle b is rows
 // [32b, 32b+32); one whose entries overflow the staging buffer is walked row
 // by row with the whole warp.
+//
+// Latency structure of a bundle: its row bounds (one coalesced load per
+// lane) -> the column indices (coalesced over the bundle's entries) and, in
+// the FMA form, the row's first kSpmvHeld values -> the x gathers -> the row
+// sums.  init() and the epilogue's loads are issued with the row bounds.
 template <typename T, bool EXACT, typename XF, typename EP>
 __device__ __forceinline__ void spmv_bundle(int b, int n, const int* __restrict__ bundles,
                                             const int* __restrict__ ia,
@@ -56,20 +79,40 @@ __device__ __forceinline__ void spmv_bundle(int b, int n, const int* __restrict_
     r0 = b * 32;
     r1 = min(r0 + 32, n);
   }
-  const int j0 = __ldg(ia + r0), j1 = __ldg(ia + r1);
-  if (j1 - j0 > kBundleNnz) {
-    for (int r = r0; r < r1; ++r) {
-      const int k0 = __ldg(ia + r), k1 = __ldg(ia + r + 1);
+  const int nr = r1 - r0;
+  const int r = r0 + lane;
+  const bool own = lane < nr;
+  // this lane's row bounds; lane nr-1's end is the bundle's
+  const int rs = own ? __ldg(ia + r) : 0;
+  const int re = own ? __ldg(ia + r + 1) : 0;
+  const int j0 = __shfl_sync(0xffffffffu, rs, 0);
+  const int j1 = __shfl_sync(0xffffffffu, re, nr - 1);
+  if (j1 - j0 > (GB_SPMV_STAGE_A && !EXACT ? kBundleNnz / 2 : kBundleNnz)) {
+    for (int rr = r0; rr < r1; ++rr) {
+      const int k0 = __ldg(ia + rr), k1 = __ldg(ia + rr + 1);
       T s = T(0);
       for (int j = k0 + lane; j < k1; j += 32) {
         const T xv = xf(__ldg(ja + j));
         s = EXACT ? add_rn(s, mul_rn(mul_rn(alpha, __ldg(a + j)), xv)) : fma_rn(__ldg(a + j), xv, s);
       }
       s = warp_sum(s);
-      if (lane == 0) ep.store(r, add_rn(ep.init(r), s));
+      if (lane == 0) {
+        ep_prefetch(ep, rr, 0);
+        ep.store(rr, add_rn(ep.init(rr), s));
+      }
     }
     __syncwarp();
     return;
+  }
+  T acc = T(0);
+  T held[kSpmvHeld];
+  if (own) {
+    ep_prefetch(ep, r, 0);
+    acc = ep.init(r);
+    if (!EXACT && !GB_SPMV_STAGE_A) {
+#pragma unroll
+      for (int u = 0; u < kSpmvHeld; ++u) held[u] = rs + u < re ? __ldg(a + rs + u) : T(0);
+    }
   }
   // staging, 4 entries per lane in flight: all index/value loads of a group
   // are issued before its x gathers, which are issued before any use
@@ -81,7 +124,7 @@ __device__ __forceinline__ void spmv_bundle(int b, int n, const int* __restrict_
     for (int u = 0; u < 4; ++u) {
       const int e = e0 + u * 32 + lane;
       c[u] = e < cnt ? __ldg(ja + j0 + e) : -1;
-      if (EXACT) av[u] = e < cnt ? __ldg(a + j0 + e) : T(0);
+      if (EXACT || GB_SPMV_STAGE_A) av[u] = e < cnt ? __ldg(a + j0 + e) : T(0);
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) xv[u] = c[u] >= 0 ? xf(c[u]) : T(0);
@@ -89,17 +132,21 @@ __device__ __forceinline__ void spmv_bundle(int b, int n, const int* __restrict_
     for (int u = 0; u < 4; ++u) {
       const int e = e0 + u * 32 + lane;
       if (e < cnt) stage[e] = EXACT ? mul_rn(mul_rn(alpha, av[u]), xv[u]) : xv[u];
+      if (!EXACT && GB_SPMV_STAGE_A && e < cnt) stage[kBundleNnz / 2 + e] = av[u];
     }
   }
   __syncwarp();
-  const int r = r0 + lane;
-  if (r < r1) {
-    const int e0 = __ldg(ia + r) - j0, e1 = __ldg(ia + r + 1) - j0;
-    T acc = ep.init(r);
+  if (own) {
+    const int e0 = rs - j0, e1 = re - j0;
     if (EXACT) {
       for (int e = e0; e < e1; ++e) acc = add_rn(acc, stage[e]);
+    } else if (GB_SPMV_STAGE_A) {
+      for (int e = e0; e < e1; ++e) acc = fma_rn(stage[kBundleNnz / 2 + e], stage[e], acc);
     } else {
-      for (int e = e0; e < e1; ++e) acc = fma_rn(__ldg(a + j0 + e), stage[e], acc);
+#pragma unroll
+      for (int u = 0; u < kSpmvHeld; ++u)
+        if (e0 + u < e1) acc = fma_rn(held[u], stage[e0 + u], acc);
+      for (int e = e0 + kSpmvHeld; e < e1; ++e) acc = fma_rn(__ldg(a + j0 + e), stage[e], acc);
     }
     ep.store(r, acc);
   }

@@ -148,7 +148,7 @@ static void system_free(gb_system s) {
                   s->v64.s, s->v32.x, s->v32.r, s->v32.w, s->v32.p0, s->v32.p1, s->v32.q,
                   s->v32.t, s->v32.s, s->b_int, s->aux1, s->aux2, s->aux3, s->part, s->st,
                   s->st_out, s->hist, s->err, s->lower_idx, s->lower_row, s->lmap_cpu,
-                  s->umap_cpu, s->scratch, s->edge_idx, s->edge_row};
+                  s->umap_cpu, s->scratch, s->edge_idx, s->edge_row, s->pv_l, s->pv_u, s->hash_dev};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->st_host) cudaFreeHost(s->st_host);
@@ -179,12 +179,19 @@ static int validate_csr(int n, int nnz, const std::vector<int>& ia, const std::v
   return GB_OK;
 }
 
-static int setup_values(gb_system s) {
+// A's derived arrays: diagonal, its reciprocal (FP64, FP32), FP32 values.
+static int setup_matrix_values(gb_system s) {
   const int n = s->n;
   GB_TRY(gather_values(n, s->dpos, s->a, s->diag, nullptr, s->s));
   GB_TRY(reciprocal_dev(n, s->diag, s->d_r, s->s));
   GB_TRY(cast_f64_to_f32(n, s->d_r, s->d_r32, s->s));
   GB_TRY(cast_f64_to_f32(s->nnz, s->a, s->a32, s->s));
+  return GB_OK;
+}
+
+static int setup_values(gb_system s) {
+  const int n = s->n;
+  GB_TRY(setup_matrix_values(s));
   if (s->prec == GB_PREC_GS_STD) {
     GB_TRY(tri_plan_fill(&s->L, s->a, s->a, kFillFma64, s->s));
     GB_TRY(tri_plan_fill(&s->U, s->a, s->a, kFillFma64, s->s));
@@ -287,6 +294,25 @@ extern "C" int gb_system_create(int n, int nnz, const int* ia, const int* ja, co
     CK(tri_plan_build(dl, &s->L32, t32l, tri_consumer_warps(4)));
     CK(tri_plan_build(du, &s->U32, t32u, tri_consumer_warps(4)));
   }
+  if (prec == GB_PREC_GS_STD) {
+    // LAP's CUDA driver hands GS_std its L and U with the diagonal inside:
+    // last in each L row, first in each U row (cg_driver2.c:95-144)
+    std::vector<int> lp(n + 1, 0), up(n + 1, 0), lj, uj;
+    for (int i = 0; i < n; ++i) {
+      for (int q = hia[i]; q < hia[i + 1]; ++q)
+        if (hja[q] < i) lj.push_back(hja[q]);
+      lj.push_back(i);
+      uj.push_back(i);
+      for (int q = hia[i]; q < hia[i + 1]; ++q)
+        if (hja[q] > i) uj.push_back(hja[q]);
+      lp[i + 1] = (int)lj.size();
+      up[i + 1] = (int)uj.size();
+    }
+    s->pl_nnz = (int)lj.size();
+    s->pu_nnz = (int)uj.size();
+    s->pat_l = pattern_hash_host(n, s->pl_nnz, lp.data(), lj.data());
+    s->pat_u = pattern_hash_host(n, s->pu_nnz, up.data(), uj.data());
+  }
   if (prec == GB_PREC_IT_JACOBI || prec == GB_PREC_GS_IT || prec == GB_PREC_GS_IT2) {
     std::vector<int> lp(n + 1, 0), up(n + 1, 0), lj, uj, lm, um;
     for (int i = 0; i < n; ++i) {
@@ -299,6 +325,10 @@ extern "C" int gb_system_create(int n, int nnz, const int* ia, const int* ja, co
     }
     s->lnnz = (int)lj.size();
     s->unnz = (int)uj.size();
+    s->pl_nnz = s->lnnz;
+    s->pu_nnz = s->unnz;
+    s->pat_l = pattern_hash_host(n, s->lnnz, lp.data(), lj.data());
+    s->pat_u = pattern_hash_host(n, s->unnz, up.data(), uj.data());
     CK(dupload(&s->lia, lp));
     CK(dupload(&s->uia, up));
     CK(dupload(&s->lja, lj));
@@ -320,6 +350,7 @@ extern "C" int gb_system_create(int n, int nnz, const int* ia, const int* ja, co
   CK(dalloc(&s->st, 1));
   CK(dalloc(&s->st_out, 1));
   CK(dalloc(&s->scratch, 8));
+  CK(dalloc(&s->hash_dev, 1));
   CKC(cudaMemset(s->st, 0, sizeof(PcgState)));
   CKC(cudaMemset(s->st_out, 0, sizeof(PcgState)));
   CKC(cudaMallocHost(&s->st_host, sizeof(PcgState) * 2));
@@ -347,6 +378,97 @@ extern "C" int gb_debug_set_spin_budget(gb_system s, unsigned long long ns) {
 extern "C" int gb_system_update_values(gb_system s) {
   if (!s) return GB_BAD_INPUT;
   return setup_values(s);
+}
+
+extern "C" int gb_system_refresh_matrix(gb_system s) {
+  if (!s) return GB_BAD_INPUT;
+  GB_TRY(setup_matrix_values(s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s->s));
+  return GB_OK;
+}
+
+extern "C" int gb_system_pattern_hash(gb_system s, int n, int nnz, const int* ia, const int* ja,
+                                      unsigned long long* out) {
+  if (!s || !out) return GB_BAD_INPUT;
+  return pattern_hash(n, nnz, ia, ja, s->hash_dev, s->s, out);
+}
+
+namespace {
+// GS_std's L (diagonal last) and U (diagonal first) onto A's pattern: row i's
+// L entries are A's entries ia[i] .. dpos[i], its U entries dpos[i] .. ia[i+1]-1
+// (the layouts were checked against the system's before this runs).
+__global__ void scatter_embedded_kernel(int n, const int* __restrict__ ia, const int* __restrict__ dpos,
+                                        const int* __restrict__ lia, const double* __restrict__ la,
+                                        const int* __restrict__ uia, const double* __restrict__ ua,
+                                        double* pv_l, double* pv_u) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int a0 = ia[i], d = dpos[i], a1 = ia[i + 1], l0 = lia[i], u0 = uia[i];
+    for (int t = 0; t <= d - a0; ++t) pv_l[a0 + t] = la[l0 + t];
+    for (int t = 0; t < a1 - d; ++t) pv_u[d + t] = ua[u0 + t];
+  }
+}
+}  // namespace
+
+extern "C" int gb_system_set_prec_values(gb_system s, const int* lia, const int* lja, const double* la,
+                                         int lnnz, const int* uia, const int* uja, const double* ua,
+                                         int unnz, const double* d_r, const double* ichol_vals) {
+  if (!s) return GB_BAD_INPUT;
+  const int n = s->n;
+  auto check_lu = [&]() -> int {
+    if (!lia || !lja || !la || !uia || !uja || !ua) return GB_BAD_INPUT;
+    if (lnnz != s->pl_nnz || unnz != s->pu_nnz) return GB_BAD_INPUT;
+    unsigned long long hl = 0, hu = 0;
+    GB_TRY(pattern_hash(n, lnnz, lia, lja, s->hash_dev, s->s, &hl));
+    GB_TRY(pattern_hash(n, unnz, uia, uja, s->hash_dev, s->s, &hu));
+    return (hl == s->pat_l && hu == s->pat_u) ? GB_OK : GB_BAD_INPUT;
+  };
+  auto load_d_r = [&]() -> int {
+    if (!d_r) return GB_BAD_INPUT;
+    GB_TRY(copy_dev(n, d_r, s->d_r, s->s));
+    return cast_f64_to_f32(n, s->d_r, s->d_r32, s->s);
+  };
+  switch (s->prec) {
+    case GB_PREC_NONE:
+      break;
+    case GB_PREC_LINE_JACOBI:
+      GB_TRY(load_d_r());
+      break;
+    case GB_PREC_IT_JACOBI:
+    case GB_PREC_GS_IT:
+    case GB_PREC_GS_IT2:
+      GB_TRY(check_lu());
+      GB_TRY(load_d_r());
+      GB_TRY(copy_dev(lnnz, la, s->la, s->s));
+      GB_TRY(copy_dev(unnz, ua, s->ua, s->s));
+      break;
+    case GB_PREC_GS_STD: {
+      GB_TRY(check_lu());
+      if (!s->pv_l) GB_TRY(dalloc(&s->pv_l, s->nnz));
+      if (!s->pv_u) GB_TRY(dalloc(&s->pv_u, s->nnz));
+      const int grid = std::max(1, std::min((n + 255) / 256, reduction_grid()));
+      scatter_embedded_kernel<<<grid, 256, 0, s->s>>>(n, s->ia, s->dpos, lia, la, uia, ua, s->pv_l, s->pv_u);
+      GB_CUDA_TRY(cudaGetLastError());
+      GB_TRY(tri_plan_fill(&s->L, s->pv_l, s->pv_l, kFillFma64, s->s));
+      GB_TRY(tri_plan_fill(&s->U, s->pv_u, s->pv_u, kFillFma64, s->s));
+      GB_TRY(tri_plan_fill(&s->L32, s->pv_l, s->pv_l, kFillFma32, s->s));
+      GB_TRY(tri_plan_fill(&s->U32, s->pv_u, s->pv_u, kFillFma32, s->s));
+      break;
+    }
+    case GB_PREC_ICHOL:
+      // the factor as initialize_ichol leaves it: L in A's lower triangle
+      // (diagonal included); the upper solve reads L's entries transposed
+      if (!ichol_vals) return GB_BAD_INPUT;
+      GB_TRY(tri_plan_fill(&s->L, ichol_vals, ichol_vals, kFillFma64, s->s));
+      GB_TRY(tri_plan_fill(&s->U, ichol_vals, ichol_vals, kFillFma64, s->s));
+      GB_TRY(tri_plan_fill(&s->L32, ichol_vals, ichol_vals, kFillFma32, s->s));
+      GB_TRY(tri_plan_fill(&s->U32, ichol_vals, ichol_vals, kFillFma32, s->s));
+      s->zero_pivot_row = 0;
+      break;
+    default:
+      return GB_BAD_INPUT;
+  }
+  GB_CUDA_TRY(cudaStreamSynchronize(s->s));
+  return GB_OK;
 }
 
 extern "C" int gb_system_info(gb_system s, int* lower_levels, int* upper_levels, int* tiles) {

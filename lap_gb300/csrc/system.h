@@ -87,6 +87,11 @@ struct gb_system_s {
 
   gb_batch multi = nullptr;       // gb_pcg_solve_multi's shared-matrix batch (a chunk of up to 32)
   gb_batch multi_tail = nullptr;  // ... and the last, shorter chunk when there are more than 32
+  // preconditioner values loaded from caller arrays (gb_system_set_prec_values)
+  unsigned long long pat_l = 0, pat_u = 0;  // fingerprints of the L / U layout LAP's pdata holds
+  int pl_nnz = 0, pu_nnz = 0;                // their entry counts
+  double *pv_l = nullptr, *pv_u = nullptr;   // GS_std: la / ua scattered onto A's pattern
+  unsigned long long* hash_dev = nullptr;    // 8 bytes of scratch for pattern_hash
   gb::LoopGraph loop[3];  // [precision]
   int loop_key[3] = {-1, -1, -1};
 };

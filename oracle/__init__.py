@@ -22,6 +22,14 @@ _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 
 
+def reference_dir() -> str | None:
+    """Where LAP's sources are mounted: $LAP_REFERENCE_DIR, else the default
+    mount point of this build's container; None where neither exists (the
+    GPU hosts, which only run the prebuilt oracle)."""
+    d = os.environ.get("LAP_REFERENCE_DIR") or "/root/reference"
+    return d if os.path.isdir(d) else None
+
+
 def build(ref_dir: str | None = None, quiet: bool = True) -> None:
     """Compile liboracle*.so (always) and _ref/libref.so (when ``ref_dir`` exists)."""
     out = subprocess.DEVNULL if quiet else None

@@ -1,6 +1,6 @@
 """Regenerates the golden fixtures in this folder FROM THE REFERENCE ITSELF.
 
-Needs the LAP sources (default /root/reference) so that ``oracle/Makefile``
+Needs the LAP sources ($LAP_REFERENCE_DIR, default /root/reference) so that ``oracle/Makefile``
 can compile the reference's NOACC objects into ``oracle/_ref/libref.so``;
 every output array below is produced by the reference's own functions
 (cg(), simple_csr_matvec(), simple_*_triangular_solve(), initialize_ichol(),
@@ -47,7 +47,7 @@ def small_cases():
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-dir", default="/root/reference")
+    ap.add_argument("--ref-dir", default=os.environ.get("LAP_REFERENCE_DIR", "/root/reference"))
     args = ap.parse_args()
     oracle.build(args.ref_dir)
     R = oracle.ref_lib()
