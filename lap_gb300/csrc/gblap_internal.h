@@ -102,6 +102,9 @@ struct TriPlan {
   int *long_col = nullptr;   // [nlong]
   int *long_src = nullptr;   // [nlong]
   bool have32 = false;
+  // every record is short with at most kTriHeld dependencies (no long rows,
+  // hub parts or tail batches): the solve may run the SHORT kernel
+  bool short_only = false;
   // rows in global level order, each level padded to a multiple of 32 with
   // -1 (the IC(0) factorization walks this order)
   int *order = nullptr;

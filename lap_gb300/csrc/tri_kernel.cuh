@@ -358,7 +358,10 @@ struct RhsAhead {
   bool have = false;
 };
 
-template <typename T, bool EXACT, bool POLL, typename OP>
+// SHORT: the plan has only short records of at most kTriHeld dependencies
+// (grids, kNN graphs): the long-row, hub-part, combine and tail paths are
+// compiled out, which halves the kernel's code.
+template <typename T, bool EXACT, bool POLL, typename OP, bool SHORT = false>
 __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy, int t0, int t1,
                                              const unsigned char* rec, int lane, int* s_done,
                                              const TriLink<T>& L, const RhsAhead<OP>& ahead) {
@@ -367,7 +370,7 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
   const int* rows = reinterpret_cast<const int*>(rec + sizeof(RecHdr));
   const T* diag = reinterpret_cast<const T*>(rows + R4);
   const T* dinv = diag + R4;
-  const bool lng = (h.flags & kRecLong) != 0;
+  const bool lng = !SHORT && (h.flags & kRecLong) != 0;
   const bool act = lng ? true : lane < h.nrows;
   const int row = act ? rows[lng ? 0 : lane] : -1;
   typename OP::Pre pr;
@@ -522,7 +525,7 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
     // loads are issued before the first is consumed (a power-law row has
     // dozens, each an L2 round trip), then the terms are added in column
     // order; padding columns (-1) end the row
-    for (int k0 = kTriHeld; k0 < h.len; k0 += kTriTailBatch) {
+    for (int k0 = kTriHeld; !SHORT && k0 < h.len; k0 += kTriTailBatch) {
       int cb[kTriTailBatch];
       T lb[kTriTailBatch], vb[kTriTailBatch];
 #pragma unroll
@@ -587,7 +590,8 @@ __device__ __forceinline__ int ld_cluster_s32(uint32_t addr) {
 // per group: after the group is known, after every inbox holds the
 // sentinel (before any push), and at the end (no CTA refills or frees its
 // inbox while its predecessor may still push into it).
-template <typename T, typename OP, bool EXACT, int CL = 1, bool PULL = false, bool POLL = false>
+template <typename T, typename OP, bool EXACT, int CL = 1, bool PULL = false, bool POLL = false,
+          bool SHORT = false>
 __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArgs<T> A, OP op) {
   constexpr int kTriConsumers = TriCons<T>::n;
   constexpr int kTriThreads = TriCons<T>::threads;
@@ -744,7 +748,9 @@ __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArg
             }
           }
 #endif
-          if (!failed) solve_record<T, EXACT, POLL>(A, op, sy, t0, t1, ring + slot * kTriSlotBytes, lane, &s_done, link, cur);
+          if (!failed)
+            solve_record<T, EXACT, POLL, OP, SHORT>(A, op, sy, t0, t1, ring + slot * kTriSlotBytes, lane, &s_done,
+                                                    link, cur);
           __syncwarp();
           // after a failure the slot is not released: its copy may still be in
           // flight, and the producer must not aim another copy at it
@@ -797,10 +803,10 @@ bool tri_fp64_clusters();
 
 // GB_NOT_SUPPORTED when the device cannot place one cluster of CL CTAs, or,
 // with all_resident, cannot place every group's cluster at once.
-template <typename T, typename OP, bool EXACT, int CL, bool PULL = false, bool POLL = false>
+template <typename T, typename OP, bool EXACT, int CL, bool PULL = false, bool POLL = false, bool SHORT = false>
 int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, size_t smem,
                   bool all_resident = false) {
-  auto kern = tri_tile_kernel<T, OP, EXACT, CL, PULL, POLL>;
+  auto kern = tri_tile_kernel<T, OP, EXACT, CL, PULL, POLL, SHORT>;
   static bool attr_set = false;  // one per instantiation
   if (!attr_set) {
     GB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kTriMaxDynSmem));
@@ -896,12 +902,42 @@ int tri_launch_form(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s
 // Lower-solve OPs poll tile values where the plan's levels hold several
 // records each (A.poll); the two forms are separate instantiations, since a
 // runtime switch in the record code measured slower in both.
+// Plans of short records only (TriPlan::short_only) in the forms large
+// ones take -- thread-block clusters of 16 (pushing into an inbox where it
+// fits, else pulling) or one CTA per tile -- run the SHORT instantiation;
+// GB_NOT_SUPPORTED sends every other case to the general kernel.
+template <typename T, typename OP, bool EXACT, bool POLL>
+int tri_launch_short(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
+  const size_t smem = (size_t)kTriSlots * kTriSlotBytes + (size_t)p.tile_rows * sizeof(T);
+  const size_t smem_inbox = smem + (size_t)p.tile_rows * sizeof(T);
+  if (p.ntiles <= 0 || smem > (size_t)kTriMaxDynSmem) return GB_NOT_SUPPORTED;
+  const int want = tri_cluster_size();
+  if (p.levels_form || p.ntiles <= 8 || want == 0)
+    return p.levels_form || want == 0 ? tri_launch_cl<T, OP, EXACT, 1, false, POLL, true>(p, A, op, s, smem)
+                                      : GB_NOT_SUPPORTED;
+  if (want != 16 && want >= 0) return GB_NOT_SUPPORTED;
+  if (sizeof(T) == 4 && smem_inbox <= (size_t)kTriMaxDynSmem)
+    return tri_launch_cl<T, OP, EXACT, 16, false, POLL, true>(p, A, op, s, smem_inbox);
+  if (sizeof(T) == 4 || tri_fp64_clusters()) return tri_launch_cl<T, OP, EXACT, 16, true, POLL, true>(p, A, op, s, smem);
+  return GB_NOT_SUPPORTED;
+}
+
 template <typename T, typename OP, bool EXACT>
 int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   // split hub rows: every partial-sum slot at the sentinel before the solve
   if (p.nslots > 0) GB_TRY(fill_sentinel_dev(p.nslots, A.part, s));
   if constexpr (op_polls_values<OP>::value) {
-    if (A.poll) return tri_launch_form<T, OP, EXACT, true>(p, A, op, s);
+    if (A.poll) {
+      if (p.short_only) {
+        const int rc = tri_launch_short<T, OP, EXACT, true>(p, A, op, s);
+        if (rc != GB_NOT_SUPPORTED) return rc;
+      }
+      return tri_launch_form<T, OP, EXACT, true>(p, A, op, s);
+    }
+  }
+  if (p.short_only) {
+    const int rc = tri_launch_short<T, OP, EXACT, false>(p, A, op, s);
+    if (rc != GB_NOT_SUPPORTED) return rc;
   }
   return tri_launch_form<T, OP, EXACT, false>(p, A, op, s);
 }

@@ -339,6 +339,11 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows, int level_run
   }
   GB_TRY(upload_set(&plan->r32, buf, off, nbytes, vdst, ddst, idst, long_col.size(), 4));
 
+  plan->short_only = true;
+  for (const RecDesc& r : recs)
+    if (r.is_long || r.len > kTriHeld) plan->short_only = false;
+  if (const char* e = getenv("GBLAP_TRI_SHORT"))  // 0: always the general kernel
+    if (e[0] == '0') plan->short_only = false;
   plan->n = n;
   plan->lower = lower;
   plan->nlevels = nlev;
