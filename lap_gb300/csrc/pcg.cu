@@ -32,6 +32,10 @@
 namespace gb {
 
 constexpr int kThreads = 256;
+// grid-stride elements per step in the elementwise kernels (128^3 update:
+// 33.8 us at 1, 28.4 at 4, 39.7 at 8 -- registers then halve the resident
+// blocks; a grid of twice the blocks measured 36.6)
+constexpr int kEwUnroll = 4;
 
 template <typename T>
 struct VecPtrs {
@@ -193,17 +197,36 @@ __global__ void __launch_bounds__(kThreads)
   }
   const T al = (T)alpha, nal = (T)(-alpha);
   double acc[2] = {0.0, 0.0};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    x[i] = fma_rn(al, p[i], x[i]);
-    const T ri = fma_rn(nal, q[i], r[i]);
+  auto one = [&](int i, T pv, T xv, T qv, T rv, T dv) {
+    x[i] = fma_rn(al, pv, xv);
+    const T ri = fma_rn(nal, qv, rv);
     r[i] = ri;
     acc[0] += (double)ri * (double)ri;
     if (WK == WK_JACOBI) {
-      const T wi = d_r[i] * ri;
+      const T wi = dv * ri;
       w[i] = wi;
       acc[1] += (double)ri * (double)wi;
     }
+  };
+  // kEwUnroll grid-stride elements per step, all their loads issued first:
+  // a thread keeps kEwUnroll x 4-5 loads in flight instead of 4-5
+  const int stride = gridDim.x * blockDim.x;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + (kEwUnroll - 1) * stride < n; i += kEwUnroll * stride) {
+    T pv[kEwUnroll], xv[kEwUnroll], qv[kEwUnroll], rv[kEwUnroll], dv[kEwUnroll];
+#pragma unroll
+    for (int u = 0; u < kEwUnroll; ++u) {
+      const int j = i + u * stride;
+      pv[u] = p[j];
+      xv[u] = x[j];
+      qv[u] = q[j];
+      rv[u] = r[j];
+      dv[u] = WK == WK_JACOBI ? d_r[j] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kEwUnroll; ++u) one(i + u * stride, pv[u], xv[u], qv[u], rv[u], dv[u]);
   }
+  for (; i < n; i += stride) one(i, p[i], x[i], q[i], r[i], WK == WK_JACOBI ? d_r[i] : T(0));
   if (reduce_last<2>(acc, part, gridDim.x, blockIdx.x, &st->tk[TK_UPD], sm) && threadIdx.x == 0) {
     pcg_check(st, acc[0], hist);
     if (WK != WK_PREC) {
@@ -223,8 +246,20 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ double sm[kThreads / 32];
   if (st->done) return;
   double acc[1] = {0.0};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    acc[0] = fma((double)r[i], (double)w[i], acc[0]);
+  const int stride = gridDim.x * blockDim.x;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + (kEwUnroll - 1) * stride < n; i += kEwUnroll * stride) {
+    T rv[kEwUnroll];
+    TW wv[kEwUnroll];
+#pragma unroll
+    for (int u = 0; u < kEwUnroll; ++u) {
+      rv[u] = r[i + u * stride];
+      wv[u] = w[i + u * stride];
+    }
+#pragma unroll
+    for (int u = 0; u < kEwUnroll; ++u) acc[0] = fma((double)rv[u], (double)wv[u], acc[0]);
+  }
+  for (; i < n; i += stride) acc[0] = fma((double)r[i], (double)w[i], acc[0]);
   if (reduce_last<1>(acc, part, gridDim.x, blockIdx.x, &st->tk[TK_RHO], sm) && threadIdx.x == 0) {
     st->rho_prev = st->rho;
     st->rho = acc[0];
