@@ -916,9 +916,21 @@ int tri_launch_short(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t 
     return p.levels_form || want == 0 ? tri_launch_cl<T, OP, EXACT, 1, false, POLL, true>(p, A, op, s, smem)
                                       : GB_NOT_SUPPORTED;
   if (want != 16 && want >= 0) return GB_NOT_SUPPORTED;
-  if (sizeof(T) == 4 && smem_inbox <= (size_t)kTriMaxDynSmem)
-    return tri_launch_cl<T, OP, EXACT, 16, false, POLL, true>(p, A, op, s, smem_inbox);
-  if (sizeof(T) == 4 || tri_fp64_clusters()) return tri_launch_cl<T, OP, EXACT, 16, true, POLL, true>(p, A, op, s, smem);
+  if constexpr (sizeof(T) == 4) {
+    if (smem_inbox <= (size_t)kTriMaxDynSmem)
+      return tri_launch_cl<T, OP, EXACT, 16, false, POLL, true>(p, A, op, s, smem_inbox);
+    return tri_launch_cl<T, OP, EXACT, 16, true, POLL, true>(p, A, op, s, smem);
+  }
+  if (!tri_fp64_clusters()) return GB_NOT_SUPPORTED;
+  // FP64 lower solves in clusters of 10: two fit on most GPCs, so the 128
+  // plane tiles of a 128^3 grid are all resident (in clusters of 16 only 7
+  // groups of 16 are, and the eighth starts when the first has finished):
+  // 319 vs 360 us there; 8 / 9 / 12 measured 346 / 322 / 388.  FP64 upper
+  // and FP32 solves measured best in clusters of 16.
+  if constexpr (sizeof(T) == 8) {
+    if (p.lower) return tri_launch_cl<T, OP, EXACT, 10, true, POLL, true>(p, A, op, s, smem);
+    return tri_launch_cl<T, OP, EXACT, 16, true, POLL, true>(p, A, op, s, smem);
+  }
   return GB_NOT_SUPPORTED;
 }
 
