@@ -380,6 +380,17 @@ def run_workload(args, local):
                                      "max_iters": int(its.max()), "all_converged": bool((fl == 0).all()),
                                      "rel_true_res_max": r["rel_true_res"],
                                      "rel_err_vs_fp64": float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64))}
+        # the autotuner's plan for this batch, then the same solves on it
+        tune = bt.autotune(db, iters=16)
+        line["autotune"] = dict(tune)
+        for p in (0, 2):
+            bt.solve(db, tol=1e-8, maxit=20000, precision=p)
+            res = _timed_solves(lambda: bt.solve(db, tol=1e-8, maxit=20000, precision=p), 3)
+            x, its, fl, r = res[-1]
+            line["autotune"][f"precision{p}_ms"] = round(statistics.mean(rr["device_ms"] for *_, rr in res), 2)
+            line["autotune"][f"precision{p}_all_converged"] = bool((fl == 0).all())
+            line["autotune"][f"precision{p}_rel_err_vs_fp64"] = float(torch.linalg.norm(x - x64) /
+                                                                      torch.linalg.norm(x64))
         t2 = time.time()  # the same systems one by one with the single-system solver
         ms = 0.0
         for A, b in zip(mats, rhs):
@@ -409,6 +420,14 @@ def run_workload(args, local):
                     "rel_true_res_max": r["rel_true_res"],
                     "rel_err_vs_fp64": float(torch.linalg.norm(X - X64) / torch.linalg.norm(X64))}
             os.environ.pop("GBLAP_MULTI_FORM", None)
+        tune = gb.autotune_multi(sysm, Bm, iters=16)  # columns per interleaved chunk, by timing
+        line["autotune"] = dict(tune)
+        for p in (0, 2):
+            gb.solve_multi(sysm, Bm, tol=1e-8, maxit=20000, precision=p)
+            X, its, r = gb.solve_multi(sysm, Bm, tol=1e-8, maxit=20000, precision=p)
+            line["autotune"][f"precision{p}_ms"] = round(r["device_ms"], 2)
+            line["autotune"][f"precision{p}_rel_err_vs_fp64"] = float(torch.linalg.norm(X - X64) /
+                                                                      torch.linalg.norm(X64))
         ms = 0.0
         for k in range(Bm.shape[0]):
             _, rs = sysm.solve(Bm[k], tol=1e-8, maxit=20000)
@@ -422,7 +441,8 @@ def run_workload(args, local):
         xs = torch.from_numpy(rng.standard_normal(A.n)).cuda()
         b = torch.from_numpy(rng.uniform(-1, 1, A.n)).cuda()
         line["config"] = ("1024^2 anisotropic lognormal grid + 1e-2 I, ichol, loss 0.5||x-x*||^2; forward and "
-                          "adjoint in split precision (tol 1e-10); central differences h=1e-6 (FP64, tol 1e-13)")
+                          "adjoint in split precision (tol 1e-10); central differences h=1e-6 (FP64, tol 1e-13) "
+                          "and the reference CPU PCG's own adjoint (FP64 IC(0), tol 1e-10) on the same random edges")
         sysm = gb.System.from_csr(A, "ichol")
         kw = dict(tol=1e-10, maxit=20000, precision=2)
         sysm.solve(b, **kw)
@@ -453,6 +473,23 @@ def run_workload(args, local):
         line["fd_edges"] = int(args.fd_edges)
         line["fd_abs_err_max_over_max_grad"] = float(np.abs(fds - ads).max() / np.abs(ads).max())
         line["fd_rel_err_median"] = float(np.median(np.abs(fds - ads) / np.abs(ads)))
+        # the reference's CPU PCG (the oracle, FP64 IC(0)) for the forward and
+        # the adjoint solve; its gradient on the same edges and its dL/db
+        import oracle
+
+        t2 = time.time()
+        bn, xsn = b.cpu().numpy(), xs.cpu().numpy()
+        ref_f = oracle.solve(A.n, A.ia, A.ja, A.a, bn, "ichol", 1e-10, 20000)
+        ref_a = oracle.solve(A.n, A.ia, A.ja, A.a, ref_f["x"] - xsn, "ichol", 1e-10, 20000)
+        xr, lr = ref_f["x"], ref_a["x"]
+        g_ref = np.array([-(lr[lo[e]] - lr[hi[e]]) * (xr[lo[e]] - xr[hi[e]]) for e in edges])
+        lam_np = lam.cpu().numpy()
+        line["reference_adjoint"] = {
+            "iters": [ref_f["iters"], ref_a["iters"]], "cpu_s": round(time.time() - t2, 1),
+            "grad_abs_err_max_over_max_grad": float(np.abs(ads - g_ref).max() / np.abs(g_ref).max()),
+            "grad_rel_err_median": float(np.median(np.abs(ads - g_ref) / np.abs(g_ref))),
+            "dL_db_rel_err": float(np.linalg.norm(lam_np - lr) / np.linalg.norm(lr)),
+            "fd_vs_reference_grad_max_over_max_grad": float(np.abs(fds - g_ref).max() / np.abs(g_ref).max())}
     else:
         raise SystemExit(f"unknown workload {wl}")
     line["wall_s"] = round(time.time() - t0, 1)
@@ -627,7 +664,7 @@ def main():
                     choices=["ichol128", "jacobi256", "chunglu4m", "batch512", "multirhs32", "multirhs64", "adjoint1024",
                              "mmread128"],
                     help="ichol128 is the headline line; the others are the remaining configurations")
-    ap.add_argument("--fd-edges", type=int, default=16)
+    ap.add_argument("--fd-edges", type=int, default=64)
     ap.add_argument("--profile-precisions", default="0,1,2",
                     help="--kernels-only: precision modes to run (comma list of 0, 1, 2)")
     args = ap.parse_args()

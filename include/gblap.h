@@ -199,6 +199,26 @@ int gb_pcg_solve_multi(gb_system sys, int nrhs, const double *B, double *X,
  * matrix shape class).  best_host receives the chosen rows-per-bundle. */
 int gb_autotune_spmv(gb_system sys, int *best_host);
 
+/* Picks a block-diagonal batch's row-bundle and tile sizes by timing them:
+ * rows per SpMV bundle in {32, 16, 8} x rows per update / reduction chunk in
+ * {2048, 1024, 4096}, each running `iters` iterations (<= 0: 16) of the
+ * batch's own captured solve loop (FP64, no stopping) on right-hand side b;
+ * the fastest is applied to the batch and cached per matrix class (system
+ * count, rows, entries, longest row), so later batches of that class are set
+ * without timing.  Results of the tuned batch equal the default's up to the
+ * rounding of the regrouped reductions.  Outputs may be NULL; the times are
+ * 0 when the choice came from the cache.  GB_NOT_SUPPORTED for multi-RHS
+ * batches (see gb_pcg_autotune_multi).  No counterpart in LAP. */
+int gb_batch_autotune(gb_batch batch, const double *b, int iters, int *rows_per_bundle, int *chunk_rows,
+                      double *ms_default, double *ms_best);
+
+/* Picks the columns per interleaved chunk of gb_pcg_solve_multi for nrhs
+ * right-hand sides B ([nrhs][n], device) on this system by timing 32, 16 and
+ * 8 over `iters` iterations; the fastest is kept on the system (and cached
+ * per (n, nnz, nrhs)).  No counterpart in LAP. */
+int gb_pcg_autotune_multi(gb_system sys, int nrhs, const double *B, int iters, int *width, double *ms_default,
+                          double *ms_best);
+
 /* ------------------------------------------------------------ failure injection */
 /* Test hook: wall-clock limit (ns) of every sync-free wait in this system's
  * solves and factorization; 0 restores the default of one second.  A wait

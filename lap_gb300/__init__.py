@@ -104,6 +104,8 @@ def _proto(L: C.CDLL) -> None:
         "gb_batch_solve": (i, [vp, vp, vp, C.POINTER(PcgOpts), vp, vp, C.POINTER(PcgResult)]),
         "gb_pcg_solve_multi": (i, [vp, i, vp, vp, C.POINTER(PcgOpts), vp, C.POINTER(PcgResult)]),
         "gb_autotune_spmv": (i, [vp, C.POINTER(i)]),
+        "gb_batch_autotune": (i, [vp, vp, i, C.POINTER(i), C.POINTER(i), C.POINTER(d), C.POINTER(d)]),
+        "gb_pcg_autotune_multi": (i, [vp, i, vp, i, C.POINTER(i), C.POINTER(d), C.POINTER(d)]),
         "gb_debug_set_spin_budget": (i, [vp, C.c_ulonglong]),
         "gb_dot_noalloc": (i, [i, vp, vp, C.POINTER(C.c_double), vp]),
         "gb_mm_read_csr": (i, [C.c_char_p, C.POINTER(MmCsr)]),
@@ -364,6 +366,18 @@ class Batch:
                                    C.byref(r)), "gb_batch_solve")
         return x, it, fl, r.as_dict()
 
+    def autotune(self, b, iters: int = 16) -> dict:
+        """gb_batch_autotune: times the row-bundle / chunk choices on this
+        batch (right-hand side b) and applies the fastest."""
+        import torch
+
+        b = b.to(device="cuda", dtype=torch.float64).contiguous()
+        rpb, cr, t0, t1 = C.c_int(), C.c_int(), C.c_double(), C.c_double()
+        torch.cuda.synchronize()
+        check(lib().gb_batch_autotune(self.h, ptr(b), iters, C.byref(rpb), C.byref(cr), C.byref(t0), C.byref(t1)),
+              "gb_batch_autotune")
+        return dict(rows_per_bundle=rpb.value, chunk_rows=cr.value, ms_default=t0.value, ms_best=t1.value)
+
     def split(self, v):
         """Per-system views of a concatenated vector."""
         return [v[self.row_off[s]:self.row_off[s + 1]] for s in range(self.count)]
@@ -450,3 +464,16 @@ def solve_multi(system, B, X=None, **kw):
     check(lib().gb_pcg_solve_multi(system.h, B.shape[0], ptr(B), ptr(X), C.byref(o), it.ctypes.data,
                                    C.byref(r)), "gb_pcg_solve_multi")
     return X, it, r.as_dict()
+
+
+def autotune_multi(system, B, iters: int = 16) -> dict:
+    """gb_pcg_autotune_multi: columns per interleaved chunk for B [nrhs, n]
+    on this System, chosen by timing and kept on the system."""
+    import torch
+
+    B = B.to(device="cuda", dtype=torch.float64).contiguous()
+    w, t0, t1 = C.c_int(), C.c_double(), C.c_double()
+    torch.cuda.synchronize()
+    check(lib().gb_pcg_autotune_multi(system.h, B.shape[0], ptr(B), iters, C.byref(w), C.byref(t0), C.byref(t1)),
+          "gb_pcg_autotune_multi")
+    return dict(width=w.value, ms_default=t0.value, ms_best=t1.value)

@@ -31,6 +31,9 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "gb_common.cuh"
@@ -913,6 +916,13 @@ struct gb_batch_s {
   double loop_delta[2] = {0.0, 0.0};
   int loop_mo[2] = {-1, -1};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // block-diagonal batches: the host row pointers and system offsets the
+  // bundle and chunk tables are (re)built from, the autotuner's choices, and
+  // the partial buffers' capacities
+  std::vector<int> h_ia, h_roff;
+  int rpb = kBundleRows;       // rows per SpMV bundle
+  int chunk_rows = kChunkRows; // rows per update / reduction chunk
+  size_t part_b_cap = 0, part_c_cap = 0;
 };
 
 namespace {
@@ -949,12 +959,24 @@ void batch_free(gb_batch bt) {
   delete bt;
 }
 
-// Chunks of <= kChunkRows rows, never across systems; row_off on the host.
+// Frees a device buffer the batch owns.
+void bfree(gb_batch bt, const void* p) {
+  if (!p) return;
+  auto it = std::find(bt->owned.begin(), bt->owned.end(), const_cast<void*>(p));
+  if (it != bt->owned.end()) bt->owned.erase(it);
+  cudaFree(const_cast<void*>(p));
+}
+
+// Chunks of <= chunk_rows rows, never across systems; row_off on the host.
 int batch_chunks(gb_batch bt, const std::vector<int>& row_off) {
   std::vector<int> r0, cs, sc(bt->count + 1, 0);
+  for (const void* q : {(const void*)bt->chunk_r0, (const void*)bt->csys, (const void*)bt->sys_c,
+                        (const void*)bt->row_off})
+    bfree(bt, q);
+  bt->chunk_r0 = bt->csys = bt->sys_c = bt->row_off = nullptr;
   for (int s = 0; s < bt->count; ++s) {
     sc[s] = (int)cs.size();
-    for (int i = row_off[s]; i < row_off[s + 1]; i += kChunkRows) {
+    for (int i = row_off[s]; i < row_off[s + 1]; i += bt->chunk_rows) {
       r0.push_back(i);
       cs.push_back(s);
     }
@@ -969,6 +991,60 @@ int batch_chunks(gb_batch bt, const std::vector<int>& row_off) {
   return GB_OK;
 }
 
+// Partial-sum buffers for the current bundle and chunk counts (grown when a
+// new plan needs more).
+int batch_parts(gb_batch bt) {
+  const size_t nb = 3 * (size_t)bt->nb * (bt->shared ? bt->count : 1), nc = 2 * (size_t)bt->nc;
+  if (nb > bt->part_b_cap) {
+    bfree(bt, bt->part_b);
+    GB_TRY(balloc(bt, &bt->part_b, nb));
+    bt->part_b_cap = nb;
+  }
+  if (nc > bt->part_c_cap) {
+    bfree(bt, bt->part_c);
+    GB_TRY(balloc(bt, &bt->part_c, nc));
+    bt->part_c_cap = nc;
+  }
+  return GB_OK;
+}
+
+// Block-diagonal bundles: <= rpb rows and <= kBundleNnz entries of one
+// system; a longer row alone.
+int batch_bundles(gb_batch bt) {
+  const std::vector<int>& hia = bt->h_ia;
+  std::vector<int> bun{0}, bsys, sysb(bt->count + 1, 0);
+  for (int s = 0; s < bt->count; ++s) {
+    sysb[s] = (int)bsys.size();
+    int r = bt->h_roff[s];
+    const int end = bt->h_roff[s + 1];
+    while (r < end) {
+      const int start = r;
+      long long nz = 0;
+      if (hia[r + 1] - hia[r] > kBundleNnz) {
+        ++r;
+      } else {
+        while (r < end && r - start < bt->rpb && nz + (hia[r + 1] - hia[r]) <= kBundleNnz) {
+          nz += hia[r + 1] - hia[r];
+          ++r;
+        }
+      }
+      bun.push_back(r);
+      bsys.push_back(s);
+    }
+  }
+  sysb[bt->count] = (int)bsys.size();
+  for (const void* q : {(const void*)bt->bundles, (const void*)bt->bsys, (const void*)bt->sys_b}) bfree(bt, q);
+  bt->bundles = nullptr;
+  bt->bsys = bt->sys_b = nullptr;
+  bt->nb = (int)bsys.size();
+  int* dbun = nullptr;
+  GB_TRY(bupload(bt, &dbun, bun));
+  bt->bundles = dbun;
+  GB_TRY(bupload(bt, &bt->bsys, bsys));
+  GB_TRY(bupload(bt, &bt->sys_b, sysb));
+  return GB_OK;
+}
+
 // Vectors, states and partials.
 int batch_buffers(gb_batch bt) {
   const size_t N = bt->N;
@@ -978,8 +1054,7 @@ int batch_buffers(gb_batch bt) {
   GB_TRY(balloc(bt, &bt->st, bt->count));
   GB_TRY(balloc(bt, &bt->so, bt->count));
   GB_CUDA_TRY(cudaMallocHost(&bt->st_h, sizeof(PcgState) * 2 * bt->count));
-  GB_TRY(balloc(bt, &bt->part_b, 3 * (size_t)bt->nb * (bt->shared ? bt->count : 1)));
-  GB_TRY(balloc(bt, &bt->part_c, 2 * (size_t)bt->nc));
+  GB_TRY(batch_parts(bt));
   GB_TRY(balloc(bt, &bt->tk, 4));
   GB_TRY(balloc(bt, &bt->nactive, 4));
   GB_CUDA_TRY(cudaMemset(bt->tk, 0, sizeof(unsigned) * 4));
@@ -1263,36 +1338,11 @@ extern "C" int gb_batch_create(int count, const long long* row_off_host, const l
   };
   if (cudaStreamCreateWithFlags(&bt->s, cudaStreamNonBlocking) != cudaSuccess) return fail(GB_CUDA_ERROR);
   bt->own_stream = true;
-  // bundles per system: <= 32 rows, <= kBundleNnz entries, a longer row alone
-  std::vector<int> bun{0}, bsys, sysb(count + 1, 0), roff(count + 1);
-  for (int s = 0; s < count; ++s) {
-    roff[s] = (int)row_off_host[s];
-    sysb[s] = (int)bsys.size();
-    int r = (int)row_off_host[s];
-    const int end = (int)row_off_host[s + 1];
-    while (r < end) {
-      const int start = r;
-      long long nz = 0;
-      if (hia[r + 1] - hia[r] > kBundleNnz) {
-        ++r;
-      } else {
-        while (r < end && r - start < kBundleRows && nz + (hia[r + 1] - hia[r]) <= kBundleNnz) {
-          nz += hia[r + 1] - hia[r];
-          ++r;
-        }
-      }
-      bun.push_back(r);
-      bsys.push_back(s);
-    }
-  }
-  roff[count] = N;
-  sysb[count] = (int)bsys.size();
-  bt->nb = (int)bsys.size();
-  int* dbun = nullptr;
-  if ((rc = bupload(bt, &dbun, bun)) != GB_OK) return fail(rc);
-  bt->bundles = dbun;
-  if ((rc = bupload(bt, &bt->bsys, bsys)) != GB_OK || (rc = bupload(bt, &bt->sys_b, sysb)) != GB_OK ||
-      (rc = batch_chunks(bt, roff)) != GB_OK || (rc = batch_buffers(bt)) != GB_OK)
+  bt->h_roff.resize(count + 1);
+  for (int s = 0; s <= count; ++s) bt->h_roff[s] = (int)row_off_host[s];
+  bt->h_ia = std::move(hia);
+  if ((rc = batch_bundles(bt)) != GB_OK || (rc = batch_chunks(bt, bt->h_roff)) != GB_OK ||
+      (rc = batch_buffers(bt)) != GB_OK)
     return fail(rc);
   // 1/diag and the FP32 values
   const int nnz = (int)nnz_off_host[count];
@@ -1418,22 +1468,24 @@ extern "C" int gb_pcg_solve_multi(gb_system sys, int nrhs, const double* B, doub
     GB_TRY(multi_batch(sys, &sys->multi, nrhs, false, &bt));
     return batch_solve(bt, B, X, opts, iters_host, nullptr, result);
   }
-  if (nrhs <= kIlMaxRhs) {
+  const int width = sys->multi_width > 0 ? sys->multi_width : kIlMaxRhs;
+  if (nrhs <= width) {
     gb_batch bt = nullptr;
     GB_TRY(multi_batch(sys, &sys->multi, nrhs, true, &bt));
     return batch_solve(bt, B, X, opts, iters_host, nullptr, result);
   }
-  // chunks of 32 columns and a last, shorter one, each an interleaved solve
-  // that reads the matrix once per iteration for its columns; the result
-  // aggregates the chunks as one solve's does its columns
+  // chunks of `width` columns (32 unless the autotuner chose fewer) and a
+  // last, shorter one, each an interleaved solve that reads the matrix once
+  // per iteration for its columns; the result aggregates the chunks as one
+  // solve's does its columns
   gb_pcg_result acc;
   memset(&acc, 0, sizeof acc);
   acc.status = GB_OK;
   const size_t n = (size_t)sys->n;
-  for (int c0 = 0; c0 < nrhs; c0 += kIlMaxRhs) {
-    const int c = std::min(kIlMaxRhs, nrhs - c0);
+  for (int c0 = 0; c0 < nrhs; c0 += width) {
+    const int c = std::min(width, nrhs - c0);
     gb_batch bt = nullptr;
-    GB_TRY(multi_batch(sys, c == kIlMaxRhs ? &sys->multi : &sys->multi_tail, c, true, &bt));
+    GB_TRY(multi_batch(sys, c == width ? &sys->multi : &sys->multi_tail, c, true, &bt));
     gb_pcg_result r;
     GB_TRY(batch_solve(bt, B + (size_t)c0 * n, X + (size_t)c0 * n, opts, iters_host ? iters_host + c0 : nullptr,
                        nullptr, &r));
@@ -1448,5 +1500,170 @@ extern "C" int gb_pcg_solve_multi(gb_system sys, int nrhs, const double* B, doub
     acc.device_ms += r.device_ms;
   }
   if (result) *result = acc;
+  return GB_OK;
+}
+
+// ------------------------------------------------------------ autotuner
+// The batch's tile and row-bundle choices, picked by timing them: each
+// candidate runs `iters` iterations of the solve loop the batch really uses
+// (the captured CUDA-graph while loop, FP64, tol 0 so no system stops), and
+// the fastest is kept.  Choices are cached per matrix class, so a second
+// batch of the same shape is tuned without timing.
+namespace {
+struct BatchClass {
+  int count, N, nnz, maxrow;
+  bool operator<(const BatchClass& o) const {
+    return std::tie(count, N, nnz, maxrow) < std::tie(o.count, o.N, o.nnz, o.maxrow);
+  }
+};
+std::mutex g_btune_mu;
+auto& g_btune = *new std::map<BatchClass, std::pair<int, int>>;              // -> (rows per bundle, chunk rows)
+auto& g_mtune = *new std::map<std::tuple<int, int, int>, int>;                // (n, nnz, nrhs) -> width
+
+void batch_drop_graphs(gb_batch bt) {
+  for (int k = 0; k < 2; ++k) {
+    if (bt->loop[k].exec) cudaGraphExecDestroy(bt->loop[k].exec);
+    if (bt->loop[k].graph) cudaGraphDestroy(bt->loop[k].graph);
+    bt->loop[k] = LoopGraph();
+    bt->loop_maxit[k] = -1;
+  }
+}
+
+int batch_replan(gb_batch bt, int rpb, int chunk_rows) {
+  if (rpb == bt->rpb && chunk_rows == bt->chunk_rows) return GB_OK;
+  GB_CUDA_TRY(cudaStreamSynchronize(bt->s));
+  bt->rpb = rpb;
+  bt->chunk_rows = chunk_rows;
+  GB_TRY(batch_bundles(bt));
+  GB_TRY(batch_chunks(bt, bt->h_roff));
+  GB_TRY(batch_parts(bt));
+  batch_drop_graphs(bt);
+  return GB_OK;
+}
+
+// Device time of `iters` FP64 iterations of every system (the first run
+// captures the loop graph; the second is timed).
+int batch_time(gb_batch bt, const double* b, double* x, int iters, double* ms) {
+  gb_pcg_opts o;
+  gb_pcg_opts_default(&o);
+  o.tol = 0.0;
+  o.maxit = iters;
+  gb_pcg_result r;
+  for (int k = 0; k < 2; ++k) {
+    GB_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * (size_t)bt->N, bt->s));
+    GB_TRY(batch_solve(bt, b, x, &o, nullptr, nullptr, &r));
+  }
+  *ms = r.device_ms;
+  return GB_OK;
+}
+}  // namespace
+
+extern "C" int gb_batch_autotune(gb_batch bt, const double* b, int iters, int* rows_per_bundle, int* chunk_rows,
+                                 double* ms_default, double* ms_best) {
+  if (!bt || !b) return GB_BAD_INPUT;
+  if (bt->shared) return GB_NOT_SUPPORTED;  // multi-RHS: gb_pcg_autotune_multi
+  if (iters <= 0) iters = 16;
+  int maxrow = 0;
+  for (int i = 0; i < bt->N; ++i) maxrow = std::max(maxrow, bt->h_ia[i + 1] - bt->h_ia[i]);
+  const BatchClass key{bt->count, bt->N, bt->h_ia[bt->N], maxrow};
+  std::pair<int, int> best{kBundleRows, kChunkRows};
+  double t_def = 0.0, t_best = 0.0;
+  bool cached = false;
+  {
+    std::lock_guard<std::mutex> lk(g_btune_mu);
+    auto f = g_btune.find(key);
+    if (f != g_btune.end()) {
+      best = f->second;
+      cached = true;
+    }
+  }
+  if (!cached) {
+    double* x = nullptr;
+    GB_CUDA_TRY(cudaMalloc(&x, sizeof(double) * std::max(bt->N, 1)));
+    int rc = GB_OK;
+    t_best = 1e300;
+    for (int rpb : {kBundleRows, 16, 8}) {
+      for (int cr : {kChunkRows, 1024, 4096}) {
+        double ms = 0.0;
+        rc = batch_replan(bt, rpb, cr);
+        if (rc == GB_OK) rc = batch_time(bt, b, x, iters, &ms);
+        if (rc != GB_OK) break;
+        if (rpb == kBundleRows && cr == kChunkRows) t_def = ms;
+        if (ms < t_best) {
+          t_best = ms;
+          best = {rpb, cr};
+        }
+      }
+      if (rc != GB_OK) break;
+    }
+    cudaFree(x);
+    if (rc != GB_OK) {
+      batch_replan(bt, kBundleRows, kChunkRows);
+      return rc;
+    }
+    std::lock_guard<std::mutex> lk(g_btune_mu);
+    g_btune[key] = best;
+  }
+  GB_TRY(batch_replan(bt, best.first, best.second));
+  if (rows_per_bundle) *rows_per_bundle = best.first;
+  if (chunk_rows) *chunk_rows = best.second;
+  if (ms_default) *ms_default = t_def;
+  if (ms_best) *ms_best = t_best;
+  return GB_OK;
+}
+
+extern "C" int gb_pcg_autotune_multi(gb_system sys, int nrhs, const double* B, int iters, int* width,
+                                     double* ms_default, double* ms_best) {
+  if (!sys || nrhs <= 0 || !B) return GB_BAD_INPUT;
+  if (sys->prec != GB_PREC_LINE_JACOBI && sys->prec != GB_PREC_NONE) return GB_NOT_SUPPORTED;
+  if (iters <= 0) iters = 16;
+  const auto key = std::make_tuple(sys->n, sys->nnz, nrhs);
+  int best = kIlMaxRhs;
+  double t_def = 0.0, t_best = 0.0;
+  bool cached = false;
+  {
+    std::lock_guard<std::mutex> lk(g_btune_mu);
+    auto f = g_mtune.find(key);
+    if (f != g_mtune.end()) {
+      best = f->second;
+      cached = true;
+    }
+  }
+  if (!cached) {
+    double* X = nullptr;
+    GB_CUDA_TRY(cudaMalloc(&X, sizeof(double) * (size_t)nrhs * sys->n));
+    gb_pcg_opts o;
+    gb_pcg_opts_default(&o);
+    o.tol = 0.0;
+    o.maxit = iters;
+    int rc = GB_OK;
+    t_best = 1e300;
+    const int saved = sys->multi_width;
+    for (int w : {kIlMaxRhs, 16, 8}) {
+      if (w != kIlMaxRhs && w >= nrhs) continue;  // one chunk either way
+      sys->multi_width = w;
+      gb_pcg_result r;
+      for (int k = 0; k < 2 && rc == GB_OK; ++k) {
+        rc = cudaMemsetAsync(X, 0, sizeof(double) * (size_t)nrhs * sys->n, sys->s) == cudaSuccess ? GB_OK
+                                                                                                 : GB_CUDA_ERROR;
+        if (rc == GB_OK) rc = gb_pcg_solve_multi(sys, nrhs, B, X, &o, nullptr, &r);
+      }
+      if (rc != GB_OK) break;
+      if (w == kIlMaxRhs) t_def = r.device_ms;
+      if (r.device_ms < t_best) {
+        t_best = r.device_ms;
+        best = w;
+      }
+    }
+    sys->multi_width = saved;
+    cudaFree(X);
+    if (rc != GB_OK) return rc;
+    std::lock_guard<std::mutex> lk(g_btune_mu);
+    g_mtune[key] = best;
+  }
+  sys->multi_width = best;
+  if (width) *width = best;
+  if (ms_default) *ms_default = t_def;
+  if (ms_best) *ms_best = t_best;
   return GB_OK;
 }

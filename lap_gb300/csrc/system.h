@@ -87,6 +87,7 @@ struct gb_system_s {
 
   gb_batch multi = nullptr;       // gb_pcg_solve_multi's shared-matrix batch (a chunk of up to 32)
   gb_batch multi_tail = nullptr;  // ... and the last, shorter chunk when there are more than 32
+  int multi_width = 0;            // columns per interleaved chunk (0: 32; gb_pcg_autotune_multi)
   // preconditioner values loaded from caller arrays (gb_system_set_prec_values)
   unsigned long long pat_l = 0, pat_u = 0;  // fingerprints of the L / U layout LAP's pdata holds
   int pl_nnz = 0, pu_nnz = 0;                // their entry counts

@@ -205,3 +205,47 @@ def test_multi_rhs_unsupported_preconditioner():
     with pytest.raises(gb.GbError):
         gb.solve_multi(sysm, dev(np.stack([b, b])))
     sysm.close()
+
+
+def test_batch_autotune_same_results_no_slower():
+    """gb_batch_autotune times rows-per-bundle x chunk-row choices on the
+    batch's own loop and applies the fastest: the tuned batch converges like
+    the default one (every system, iterations +-1) to the same solutions (to
+    the rounding of the regrouped reductions), the chosen plan timed no
+    slower than the default, and a second batch of the same class takes the
+    cached choice without timing; split precision works on the tuned plan."""
+    mats, rhs = _mixed_batch(seed=11)
+    b = dev(np.concatenate(rhs))
+    bt = gb.Batch(mats, "line_jacobi")
+    x0, it0, f0, _ = bt.solve(b, tol=1e-10, maxit=20000)
+    t = bt.autotune(b, iters=12)
+    assert t["rows_per_bundle"] in (32, 16, 8) and t["chunk_rows"] in (1024, 2048, 4096)
+    assert 0.0 < t["ms_best"] <= t["ms_default"], t
+    x1, it1, f1, _ = bt.solve(b, tol=1e-10, maxit=20000)
+    assert (f0 == 0).all() and (f1 == 0).all()
+    assert np.abs(it1 - it0).max() <= 1, (it0, it1)
+    assert float(torch.linalg.norm(x1 - x0) / torch.linalg.norm(x0)) < 1e-8
+    xs, _, fs, rs = bt.solve(b, tol=1e-10, maxit=20000, precision=2)
+    assert (fs == 0).all() and rs["rel_true_res"] < 1e-10 * 1.01
+    bt2 = gb.Batch(mats, "line_jacobi")
+    t2 = bt2.autotune(b, iters=12)
+    assert (t2["rows_per_bundle"], t2["chunk_rows"]) == (t["rows_per_bundle"], t["chunk_rows"])
+    assert t2["ms_default"] == 0.0 and t2["ms_best"] == 0.0  # from the cache
+    x2, *_ = bt2.solve(b, tol=1e-10, maxit=20000)
+    assert torch.equal(x2, x1)  # the same plan: bitwise the same result
+    bt.close()
+    bt2.close()
+
+
+def test_multi_rhs_autotune_same_results_no_slower():
+    A, _ = gen.grid3d_lognormal(16, seed=5)
+    B = dev(gen.multi_rhs(A.n, 40, seed=1005))
+    s = gb.System.from_csr(A, "line_jacobi")
+    X0, it0, r0 = gb.solve_multi(s, B, tol=1e-10, maxit=5000)
+    t = gb.autotune_multi(s, B, iters=12)
+    assert t["width"] in (32, 16, 8) and 0.0 < t["ms_best"] <= t["ms_default"], t
+    X1, it1, r1 = gb.solve_multi(s, B, tol=1e-10, maxit=5000)
+    assert r0["flag"] == 0 and r1["flag"] == 0
+    assert np.abs(it1 - it0).max() <= 1
+    assert float(torch.linalg.norm(X1 - X0) / torch.linalg.norm(X0)) < 1e-8
+    s.close()
