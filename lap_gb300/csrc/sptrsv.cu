@@ -121,6 +121,15 @@ int deps_ichol(int n, const int* ia, const int* ja, const std::vector<int>& tpos
 // order pads every level to a multiple of 32); a row waits for its
 // dependencies' done flags (acquire) and publishes its own (release).
 constexpr int kFactorWarps = 8;
+// Rows whose upper part is longer than kSkipMin entries search it through a
+// coarse index in shared memory first: every stride-th column (at most
+// kSkip of them), so a lookup costs ~10 shared-memory steps and then a
+// bisection inside one window of stride entries (one or two cache lines)
+// instead of ~17 dependent loads across the whole row.  Power-law hub rows
+// (tens of thousands of entries, each updated by tens of thousands of
+// dependencies) are what this is for.
+constexpr int kSkip = 1024;
+constexpr int kSkipMin = 256;
 static_assert(32 % kFactorWarps == 0, "a group must lie inside one padded level");
 // Wall-clock limit of one wait in the factorization: a power-law graph's hub
 // rows carry tens of thousands of dependencies each and chain through one
@@ -153,6 +162,7 @@ __global__ void __launch_bounds__(kFactorWarps * 32)
                         const int* __restrict__ tpos, double* f, int* done, unsigned* ticket,
                         int* zero_pivot, int* err) {
   __shared__ int s_group;
+  __shared__ int s_skip[kFactorWarps][kSkip];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int ngroups = ceil_div(norder, kFactorWarps);
   while (true) {
@@ -166,6 +176,16 @@ __global__ void __launch_bounds__(kFactorWarps * 32)
     if (j < 0) continue;  // level padding (warp-uniform)
     const int d = dpos[j], je = ia[j + 1];
     bool ok = true;
+    // coarse index of row j's upper columns (long rows only)
+    const int ulen = je - d;
+    int stride = 0, nsk = 0;
+    if (ulen > kSkipMin) {
+      stride = max(32, (ulen + kSkip - 1) / kSkip);
+      nsk = (ulen + stride - 1) / stride;
+      __syncwarp();  // the previous row's lookups are done with s_skip
+      for (int q = lane; q < nsk; q += 32) s_skip[wid][q] = ja[d + q * stride];
+      __syncwarp();
+    }
     // dependencies i = ja[k] < j, ascending, 32 at a time: lane t reads the
     // done flag (acquire), u_ij and row i's end of dependency k0 + t in
     // parallel; a dependency not finished yet is then awaited in its turn
@@ -192,6 +212,17 @@ __global__ void __launch_bounds__(kFactorWarps * 32)
         for (int l = m + lane; l < ie; l += 32) {
           const int c = ja[l];
           int lo = d, hi = je - 1;  // bisection for column c in row j's upper part
+          if (stride) {
+            // the last index entry <= c (entry 0 is j itself, and c >= j)
+            int a = 0, b = nsk - 1;
+            while (a < b) {
+              const int mid = (a + b + 1) >> 1;
+              if (s_skip[wid][mid] <= c) a = mid;
+              else b = mid - 1;
+            }
+            lo = d + a * stride;
+            hi = min(lo + stride - 1, je - 1);
+          }
           while (lo < hi) {
             const int mid = (lo + hi) >> 1;
             if (ja[mid] < c) lo = mid + 1;
