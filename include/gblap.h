@@ -26,7 +26,8 @@ typedef enum {
   GB_BAD_INPUT = 5,    /* malformed CSR, missing diagonal, bad sizes, unknown name */
   GB_CUDA_ERROR = 6,
   GB_NO_MEMORY = 7,
-  GB_NOT_SUPPORTED = 8
+  GB_NOT_SUPPORTED = 8,
+  GB_INTERNAL = 9      /* a device-side consistency check failed (a staged record was not the one expected) */
 } gb_status;
 
 /* Preconditioner names are LAP's (prec.c:6-45). */

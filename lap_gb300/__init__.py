@@ -23,7 +23,7 @@ LIB_PATH = os.path.join(HERE, "libgblap.so")
 
 PRECONDITIONERS = ("none", "line_jacobi", "it_jacobi", "GS_std", "GS_it", "GS_it2", "ichol")
 STATUS = {0: "ok", 1: "maxit", 2: "breakdown", 3: "zero_pivot", 4: "timeout", 5: "bad_input",
-          6: "cuda_error", 7: "no_memory", 8: "not_supported"}
+          6: "cuda_error", 7: "no_memory", 8: "not_supported", 9: "internal"}
 
 _lib: C.CDLL | None = None
 

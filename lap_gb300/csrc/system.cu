@@ -34,6 +34,7 @@ extern "C" const char* gb_status_str(int s) {
     case GB_CUDA_ERROR: return "CUDA error";
     case GB_NO_MEMORY: return "out of device memory";
     case GB_NOT_SUPPORTED: return "not supported";
+    case GB_INTERNAL: return "device-side consistency check failed";
   }
   return "unknown status";
 }
@@ -762,7 +763,7 @@ static int solve_internal(gb_system s, const gb_pcg_opts* o, gb_pcg_result* res,
     for (int i = 0; i <= std::min(r.iters, hist_len - 1); ++i)
       printf("CG: it %d, res norm %5.5e \n", i, hist_host[i]);
   if (res) *res = r;
-  return r.status == GB_TIMEOUT ? GB_TIMEOUT : GB_OK;
+  return (r.status == GB_TIMEOUT || r.status == GB_INTERNAL) ? r.status : GB_OK;
 }
 
 extern "C" int gb_pcg_solve(gb_system s, const double* b, double* x, const gb_pcg_opts* opts,

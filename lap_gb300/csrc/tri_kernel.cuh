@@ -70,9 +70,22 @@ namespace gb {
 #ifndef GB_TRI_RHS_AHEAD
 #define GB_TRI_RHS_AHEAD 1
 #endif
-template <typename T>
+// The short-record kernel (SHORT below) has its own counts.  FP32: 15 as
+// well (23 and 31 warps, at 85 and 64 registers without spills, measured
+// slower on the 128^3 IC(0) solves: lower 285 / 306 us against 257).
+// FP64: 12 (128^3 FP64 lower / upper 298 / 339 us; 8 warps 321 / 364, 15
+// warps 308 / 340): its records are short enough that more warps in flight
+// outweigh the queueing on the FP64 pipe.
+#ifndef GB_TRI_CONSUMERS32S
+#define GB_TRI_CONSUMERS32S GB_TRI_CONSUMERS32
+#endif
+#ifndef GB_TRI_CONSUMERS64S
+#define GB_TRI_CONSUMERS64S 12
+#endif
+template <typename T, bool SHORT = false>
 struct TriCons {
-  static constexpr int n = sizeof(T) == 8 ? 8 : GB_TRI_CONSUMERS32;
+  static constexpr int n = sizeof(T) == 8 ? (SHORT ? GB_TRI_CONSUMERS64S : 8)
+                                          : (SHORT ? GB_TRI_CONSUMERS32S : GB_TRI_CONSUMERS32);
   static constexpr int threads = (n + 1) * 32;  // + one producer warp
 };
 constexpr int kTriSlots = 40;                          // ring depth (records in flight)
@@ -98,7 +111,8 @@ constexpr int kTriPartDeps = 1024;
 //   int rows[R4]; T diag[R4]; T dinv[R4]; int cols[len*R4]; T vals[len*R4]
 // (LONG records: no cols/vals; they live at long_col/long_val[off ...]).
 // wait_for = number of the tile's records in earlier tile-levels: the record
-// may start once that many records of the tile are complete.
+// may start once that many records of the tile are complete.  pad0 = the
+// record's index in the plan, which a consumer checks in the staged copy.
 struct RecHdr {
   int nrows, len, flags, off, wait_for, pad0, pad1, pad2;
 };
@@ -156,6 +170,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
       : "r"(smem_u32(b)), "r"(parity)
       : "memory");
   return ok != 0;
+}
+// Bounded wait until the producer has issued stream record u into its slot
+// (s_last_u[slot] == u); false on timeout / abort.  A consumer waits for this
+// before the slot's full barrier: the barrier's parity names a phase only
+// within one lap of the ring, and a consumer can reach record u while the
+// slot still holds record u - 2 * kTriSlots (its owner lags), whose phase has
+// the same parity.
+__device__ __forceinline__ bool wait_issued(const unsigned* last_u, unsigned u, int* err) {
+  if (*(const volatile unsigned*)last_u == u) return true;
+  SpinClock clk;
+  for (unsigned polls = 1;; ++polls) {
+    if (*(const volatile unsigned*)last_u == u) return true;
+    if ((polls & 63u) == 0u && clk.expired(err)) return false;
+  }
 }
 // Bounded wait on an mbarrier phase; false on timeout / abort.  The clock
 // and the (global) error word are checked only every 64 polls so that a
@@ -592,9 +620,9 @@ __device__ __forceinline__ int ld_cluster_s32(uint32_t addr) {
 // inbox while its predecessor may still push into it).
 template <typename T, typename OP, bool EXACT, int CL = 1, bool PULL = false, bool POLL = false,
           bool SHORT = false>
-__global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArgs<T> A, OP op) {
-  constexpr int kTriConsumers = TriCons<T>::n;
-  constexpr int kTriThreads = TriCons<T>::threads;
+__global__ void __launch_bounds__((TriCons<T, SHORT>::threads), 1) tri_tile_kernel(TriArgs<T> A, OP op) {
+  constexpr int kTriConsumers = TriCons<T, SHORT>::n;
+  constexpr int kTriThreads = TriCons<T, SHORT>::threads;
   extern __shared__ __align__(128) unsigned char tri_smem[];
   unsigned char* ring = tri_smem;                                     // kTriSlots x kTriSlotBytes
   T* sy = reinterpret_cast<T*>(tri_smem + kTriSlots * kTriSlotBytes);  // tile solution
@@ -708,7 +736,7 @@ __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArg
             const long long off = q < kTriRecTable ? s_roff[q] : __ldg(A.rec_off + rec0 + q);
             mbar_expect_tx(&full_bar[slot], bytes);
             tma_load_1d(ring + slot * kTriSlotBytes, A.recbuf + off, bytes, &full_bar[slot]);
-            s_last_u[slot] = u;
+            *(volatile unsigned*)&s_last_u[slot] = u;  // polled by the consumers (wait_issued)
             // after the first record is on its way: warm L2 with the vectors
             // this tile's rows read (HBM latency off the records' path)
             if (n == 1) op.prefetch(t0, t1, lane);
@@ -723,9 +751,13 @@ __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArg
         for (int q = wid; q < nrec; q += kTriConsumers) {
           const unsigned u = base + q;
           const int slot = u % kTriSlots;
-          if (!failed && !mbar_wait(&full_bar[slot], (u / kTriSlots) & 1u, A.err)) failed = true;
           const RhsAhead<OP> cur = next;
           next.have = false;
+          // a lane that saw this record landed while it solved its previous
+          // one (cur.have) has already waited for it
+          if (!failed && !cur.have &&
+              !(wait_issued(&s_last_u[slot], u, A.err) && mbar_wait(&full_bar[slot], (u / kTriSlots) & 1u, A.err)))
+            failed = true;
 #if GB_TRI_RHS_AHEAD
           // The next record of this warp, if it has landed: issue its
           // right-hand-side loads now, so they are in flight while this
@@ -752,6 +784,13 @@ __global__ void __launch_bounds__(TriCons<T>::threads, 1) tri_tile_kernel(TriArg
             solve_record<T, EXACT, POLL, OP, SHORT>(A, op, sy, t0, t1, ring + slot * kTriSlotBytes, lane, &s_done,
                                                     link, cur);
           __syncwarp();
+          // the staged record must have been this one (its header carries its
+          // index); otherwise the run stops with an error and the slot is not
+          // released.  Checked off the record's path.
+          if (!failed && reinterpret_cast<const RecHdr*>(ring + slot * kTriSlotBytes)->pad0 != rec0 + q) {
+            if (lane == 0) atomicCAS(A.err, 0, (int)GB_INTERNAL);
+            failed = true;
+          }
           // after a failure the slot is not released: its copy may still be in
           // flight, and the producer must not aim another copy at it
           if (lane == 0 && !failed) mbar_arrive(&empty_bar[slot]);
@@ -821,7 +860,7 @@ int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, 
     attr[0].val.clusterDim.x = CL;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
-    cfg.blockDim = dim3(TriCons<T>::threads);
+    cfg.blockDim = dim3(TriCons<T, SHORT>::threads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cfg.attrs = attr;
@@ -839,7 +878,7 @@ int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, 
     return GB_OK;
   } else {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TriCons<T>::threads, smem) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TriCons<T, SHORT>::threads, smem) != cudaSuccess ||
         per_sm < 1) {
       cudaGetLastError();
       per_sm = 1;
@@ -847,7 +886,7 @@ int tri_launch_cl(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s, 
     per_sm = per_sm < tri_blocks_per_sm() ? per_sm : tri_blocks_per_sm();
     const long long cap = (long long)device_sm_count() * per_sm;
     const int grid = (int)(A.ntiles < cap ? A.ntiles : cap);
-    kern<<<grid, TriCons<T>::threads, smem, s>>>(A, op);
+    kern<<<grid, TriCons<T, SHORT>::threads, smem, s>>>(A, op);
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
   }

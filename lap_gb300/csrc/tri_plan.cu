@@ -85,7 +85,7 @@ void layout(const TriDeps& d, const std::vector<RecDesc>& recs, int S, std::vect
     hdr[2] = r.is_long ? kRecLong : 0;
     hdr[3] = 0;
     hdr[4] = r.wait_for;
-    hdr[5] = (int)off.size() - 1;  // record index (diagnostics)
+    hdr[5] = (int)off.size() - 1;  // record index: the consumer checks the staged copy against it
     int* rows = hdr + kRecHdrBytes / 4;
     for (long long t = 0; t < R4; ++t) rows[t] = t < nrows ? r.rows[t] : -1;
     const long long diag_el = (base + kRecHdrBytes + 4 * R4) / S;  // element index of diag[0]
