@@ -272,6 +272,9 @@ __global__ void __launch_bounds__(kThreads)
 // of the solve's dependency chain): the x / r update runs before the lower
 // solve (update_kernel), r'w after the upper (rho_kernel), and GS_std's
 // right-hand side r - A t before its backward sweep (gs_rhs_kernel).
+// Measured on the 128^3 split solve: r'w fused into the FP32 upper solve's
+// epilogue (r_i loaded with the record, one FP64 FMA per row, per-tile sums)
+// took the solve from 337 to 389-397 us, against 18 us for rho_kernel.
 
 // Lower solve: the residual r is the right-hand side (rounded to the solve's
 // type in the split recurrence); also pre-fills the upper solve's output.
