@@ -955,10 +955,21 @@ int tri_launch_short(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t 
     return p.levels_form || want == 0 ? tri_launch_cl<T, OP, EXACT, 1, false, POLL, true>(p, A, op, s, smem)
                                       : GB_NOT_SUPPORTED;
   if (want != 16 && want >= 0) return GB_NOT_SUPPORTED;
+  // FP32: clusters of 16 when every group is resident at once, else of 10
+  // when that makes them all resident (two fit on most GPCs), else of 16.
+  // 128^3: the 64 upper tiles run in 16s; the 128 lower plane tiles in 10s
+  // (249 vs 257 us; 8 / 12 measured 254 / 280).
   if constexpr (sizeof(T) == 4) {
-    if (smem_inbox <= (size_t)kTriMaxDynSmem)
-      return tri_launch_cl<T, OP, EXACT, 16, false, POLL, true>(p, A, op, s, smem_inbox);
-    return tri_launch_cl<T, OP, EXACT, 16, true, POLL, true>(p, A, op, s, smem);
+    if (smem_inbox <= (size_t)kTriMaxDynSmem) {
+      int rc = tri_launch_cl<T, OP, EXACT, 16, false, POLL, true>(p, A, op, s, smem_inbox, true);
+      if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 10, false, POLL, true>(p, A, op, s, smem_inbox, true);
+      if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 16, false, POLL, true>(p, A, op, s, smem_inbox);
+      return rc;
+    }
+    int rc = tri_launch_cl<T, OP, EXACT, 16, true, POLL, true>(p, A, op, s, smem, true);
+    if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 10, true, POLL, true>(p, A, op, s, smem, true);
+    if (rc == GB_NOT_SUPPORTED) rc = tri_launch_cl<T, OP, EXACT, 16, true, POLL, true>(p, A, op, s, smem);
+    return rc;
   }
   if (!tri_fp64_clusters()) return GB_NOT_SUPPORTED;
   // FP64 lower solves in clusters of 10: two fit on most GPCs, so the 128
