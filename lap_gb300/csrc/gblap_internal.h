@@ -105,6 +105,10 @@ struct TriPlan {
   // every record is short with at most kTriHeld dependencies (no long rows,
   // hub parts or tail batches): the solve may run the SHORT kernel
   bool short_only = false;
+  // r32 in the fixed record layout (short-only plans): read only by the
+  // SHORT kernel; vdsrc[i] = the diagonal source index of value i's row
+  bool fixed32 = false;
+  int *vdsrc = nullptr;
   // rows in global level order, each level padded to a multiple of 32 with
   // -1 (the IC(0) factorization walks this order)
   int *order = nullptr;

@@ -119,6 +119,19 @@ struct RecHdr {
 constexpr int kRecHdrBytes = (int)sizeof(RecHdr);
 static_assert(kRecHdrBytes == 32, "record header layout");
 
+// Fixed layout of the FP32 records of a short-only plan (TriPlan::fixed32):
+// a 16-byte header {nrows, wait_for, record index, kFixTag} and one 48-byte block
+// per row (lane), three 16-byte words
+//   {row, c0, c1, c2} {c3, 1/d, l0/d, l1/d} {l2/d, l3/d, 0, 0}
+// (c_k = -1 past the row's dependencies).  Every offset is fixed, so a lane
+// issues all of its record's loads at once, with the header's beside them.
+constexpr int kFixHdrBytes = 16;
+constexpr int kFixLaneBytes = 48;
+// layout tag in the header: a record that lacks it is not read (the general
+// layout has a short record's entry offset, 0, in that word)
+constexpr int kFixTag = 0x31584946;
+static_assert(kFixHdrBytes + 32 * kFixLaneBytes <= 2048, "a fixed record fits a ring slot");
+
 template <typename T>
 struct TriArgs {
   int ntiles;
@@ -386,6 +399,16 @@ struct RhsAhead {
   bool have = false;
 };
 
+// The row a lane solves in a staged fixed-layout record (-1: idle lane).
+__device__ __forceinline__ int record_row_fixed(const unsigned char* rec, int lane) {
+  const int4 hd = *reinterpret_cast<const int4*>(rec);
+  const int row = *reinterpret_cast<const int*>(rec + kFixHdrBytes + lane * kFixLaneBytes);
+  return hd.w == kFixTag && lane < hd.x ? row : -1;
+}
+__device__ __forceinline__ int record_index(const unsigned char* rec, bool fixed) {
+  return fixed ? reinterpret_cast<const int*>(rec)[2] : reinterpret_cast<const RecHdr*>(rec)->pad0;
+}
+
 // SHORT: the plan has only short records of at most kTriHeld dependencies
 // (grids, kNN graphs): the long-row, hub-part, combine and tail paths are
 // compiled out, which halves the kernel's code.
@@ -585,6 +608,72 @@ __device__ __forceinline__ void solve_record(const TriArgs<T>& A, OP& op, T* sy,
   }
 }
 
+// A fixed-layout FP32 record (FMA form, at most kTriHeld dependencies per
+// row): the same arithmetic, in the same order, as solve_record's short
+// path -- y = rhs/d, minus the other tiles' terms, then the tile's, each in
+// column order -- with the header, row, columns, 1/d and values in four
+// independent shared-memory loads.
+template <bool POLL, typename OP>
+__device__ __forceinline__ void solve_record_fixed(const TriArgs<float>& A, OP& op, float* sy, int t0, int t1,
+                                                   const unsigned char* rec, int lane, int* s_done,
+                                                   const TriLink<float>& L, const RhsAhead<OP>& ahead) {
+  const int4 hd = *reinterpret_cast<const int4*>(rec);
+  const int4* lb = reinterpret_cast<const int4*>(rec + kFixHdrBytes + lane * kFixLaneBytes);
+  const int4 b0 = lb[0], b1 = lb[1], b2 = lb[2];
+  if (hd.w != kFixTag && lane == 0) atomicCAS(A.err, 0, (int)GB_INTERNAL);
+  const bool act = hd.w == kFixTag && lane < hd.x;
+  const int row = b0.x;
+  typename OP::Pre pr;
+  typename OP::DPre dp;
+  if (act) {
+    if (ahead.have) {
+      pr = ahead.pr;
+      dp = ahead.dp;
+    } else {
+      pr = op.pre(row);
+      dp = op.dpre(row);
+    }
+  }
+  const int hc[kTriHeld] = {b0.y, b0.z, b0.w, b1.x};
+  const float hl[kTriHeld] = {__int_as_float(b1.z), __int_as_float(b1.w), __int_as_float(b2.x),
+                              __int_as_float(b2.y)};
+  float hv[kTriHeld];
+  bool pend[kTriHeld];
+#pragma unroll
+  for (int k = 0; k < kTriHeld; ++k) {
+    pend[k] = act && hc[k] >= 0;
+    hv[k] = sentinel<float>();
+    if (pend[k] && (hc[k] < t0 || hc[k] >= t1)) hv[k] = other_tile_read(A, L, hc[k]);  // other tile: read early
+  }
+  float acc = 0.0f;
+  if (act) acc = op.rhs(row, pr) * __int_as_float(b1.y);
+#pragma unroll
+  for (int k = 0; k < kTriHeld; ++k) {
+    if (pend[k] && (hc[k] < t0 || hc[k] >= t1)) {
+      const float v = is_sentinel(hv[k]) ? other_tile_wait(A, L, hc[k]) : hv[k];
+      acc = fma_rn(-hl[k], v, acc);
+      pend[k] = false;
+    }
+  }
+  if constexpr (!POLL) wait_level(s_done, hd.y, A.err);
+#pragma unroll
+  for (int k = 0; k < kTriHeld; ++k)
+    if (pend[k]) hv[k] = POLL ? wait_local(sy + (hc[k] - t0), A.err) : sy[hc[k] - t0];
+#pragma unroll
+  for (int k = 0; k < kTriHeld; ++k)
+    if (pend[k]) acc = fma_rn(-hl[k], hv[k], acc);
+  const float yv = publishable(acc);
+  if (act && row >= t0 && row < t1) st_shared_volatile(sy + (row - t0), yv);  // the levels form has no tile rows
+  __syncwarp();
+  if constexpr (!POLL)
+    if (lane == 0) red_release_cta_add(s_done, 1);
+  if (act) {
+    if (L.out) st_cluster(L.out + (uint32_t)(row - t0) * (uint32_t)sizeof(float), yv);  // next tile's inbox
+    st_relaxed(A.y + row, yv);
+    op.done(row, yv, dp);
+  }
+}
+
 // ------------------------------------------------------------ clusters
 __device__ __forceinline__ unsigned cluster_rank() {
   unsigned r;
@@ -623,6 +712,9 @@ template <typename T, typename OP, bool EXACT, int CL = 1, bool PULL = false, bo
 __global__ void __launch_bounds__((TriCons<T, SHORT>::threads), 1) tri_tile_kernel(TriArgs<T> A, OP op) {
   constexpr int kTriConsumers = TriCons<T, SHORT>::n;
   constexpr int kTriThreads = TriCons<T, SHORT>::threads;
+  // short FP32 plans keep their FP32 records in the fixed layout (FMA form)
+  constexpr bool kFixed = SHORT && sizeof(T) == 4;
+  static_assert(!kFixed || !EXACT, "fixed-layout FP32 records hold the FMA form");
   extern __shared__ __align__(128) unsigned char tri_smem[];
   unsigned char* ring = tri_smem;                                     // kTriSlots x kTriSlotBytes
   T* sy = reinterpret_cast<T*>(tri_smem + kTriSlots * kTriSlotBytes);  // tile solution
@@ -771,7 +863,8 @@ __global__ void __launch_bounds__((TriCons<T, SHORT>::threads), 1) tri_tile_kern
             const unsigned un = base + qn;
             const int sn = un % kTriSlots;
             if (*(const volatile unsigned*)&s_last_u[sn] == un && mbar_try_wait(&full_bar[sn], (un / kTriSlots) & 1u)) {
-              const int rn = record_row(ring + sn * kTriSlotBytes, lane);
+              const int rn = kFixed ? record_row_fixed(ring + sn * kTriSlotBytes, lane)
+                                    : record_row(ring + sn * kTriSlotBytes, lane);
               if (rn >= 0) {
                 next.pr = op.pre(rn);
                 next.dp = op.dpre(rn);
@@ -780,14 +873,18 @@ __global__ void __launch_bounds__((TriCons<T, SHORT>::threads), 1) tri_tile_kern
             }
           }
 #endif
-          if (!failed)
-            solve_record<T, EXACT, POLL, OP, SHORT>(A, op, sy, t0, t1, ring + slot * kTriSlotBytes, lane, &s_done,
-                                                    link, cur);
+          if (!failed) {
+            if constexpr (kFixed)
+              solve_record_fixed<POLL, OP>(A, op, sy, t0, t1, ring + slot * kTriSlotBytes, lane, &s_done, link, cur);
+            else
+              solve_record<T, EXACT, POLL, OP, SHORT>(A, op, sy, t0, t1, ring + slot * kTriSlotBytes, lane, &s_done,
+                                                      link, cur);
+          }
           __syncwarp();
           // the staged record must have been this one (its header carries its
           // index); otherwise the run stops with an error and the slot is not
           // released.  Checked off the record's path.
-          if (!failed && reinterpret_cast<const RecHdr*>(ring + slot * kTriSlotBytes)->pad0 != rec0 + q) {
+          if (!failed && record_index(ring + slot * kTriSlotBytes, kFixed) != rec0 + q) {
             if (lane == 0) atomicCAS(A.err, 0, (int)GB_INTERNAL);
             failed = true;
           }
@@ -949,12 +1046,18 @@ template <typename T, typename OP, bool EXACT, bool POLL>
 int tri_launch_short(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   const size_t smem = (size_t)kTriSlots * kTriSlotBytes + (size_t)p.tile_rows * sizeof(T);
   const size_t smem_inbox = smem + (size_t)p.tile_rows * sizeof(T);
-  if (p.ntiles <= 0 || smem > (size_t)kTriMaxDynSmem) return GB_NOT_SUPPORTED;
+  if (p.ntiles <= 0) return GB_OK;
+  if (smem > (size_t)kTriMaxDynSmem) return GB_NOT_SUPPORTED;  // FP32 tiles always fit
   const int want = tri_cluster_size();
+  // The FP32 instantiations read the fixed layout only, and run every plan
+  // in it, in every form (one CTA per tile where no cluster form applies).
+  const bool fixed = sizeof(T) == 4;
+  if (fixed && !p.fixed32) return GB_NOT_SUPPORTED;
   if (p.levels_form || p.ntiles <= 8 || want == 0)
-    return p.levels_form || want == 0 ? tri_launch_cl<T, OP, EXACT, 1, false, POLL, true>(p, A, op, s, smem)
-                                      : GB_NOT_SUPPORTED;
-  if (want != 16 && want >= 0) return GB_NOT_SUPPORTED;
+    return p.levels_form || want == 0 || fixed ? tri_launch_cl<T, OP, EXACT, 1, false, POLL, true>(p, A, op, s, smem)
+                                               : GB_NOT_SUPPORTED;
+  if (want != 16 && want >= 0)
+    return fixed ? tri_launch_cl<T, OP, EXACT, 1, false, POLL, true>(p, A, op, s, smem) : GB_NOT_SUPPORTED;
   // FP32: clusters of 16 when every group is resident at once, else of 10
   // when that makes them all resident (two fit on most GPCs), else of 16.
   // 128^3: the 64 upper tiles run in 16s; the 128 lower plane tiles in 10s
@@ -988,18 +1091,23 @@ template <typename T, typename OP, bool EXACT>
 int tri_launch(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t s) {
   // split hub rows: every partial-sum slot at the sentinel before the solve
   if (p.nslots > 0) GB_TRY(fill_sentinel_dev(p.nslots, A.part, s));
+  // The short-record kernel: FP64 for short-only plans; FP32 exactly for the
+  // plans whose FP32 records are in the fixed layout (TriPlan::fixed32),
+  // which it alone reads and which the general kernel cannot.
+  const bool fixed = sizeof(T) == 4 && p.fixed32;
+  const bool use_short = sizeof(T) == 4 ? p.fixed32 : p.short_only;
   if constexpr (op_polls_values<OP>::value) {
     if (A.poll) {
-      if (p.short_only) {
+      if (use_short) {
         const int rc = tri_launch_short<T, OP, EXACT, true>(p, A, op, s);
-        if (rc != GB_NOT_SUPPORTED) return rc;
+        if (rc != GB_NOT_SUPPORTED || fixed) return rc;
       }
       return tri_launch_form<T, OP, EXACT, true>(p, A, op, s);
     }
   }
-  if (p.short_only) {
+  if (use_short) {
     const int rc = tri_launch_short<T, OP, EXACT, false>(p, A, op, s);
-    if (rc != GB_NOT_SUPPORTED) return rc;
+    if (rc != GB_NOT_SUPPORTED || fixed) return rc;
   }
   return tri_launch_form<T, OP, EXACT, false>(p, A, op, s);
 }

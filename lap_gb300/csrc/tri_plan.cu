@@ -59,11 +59,13 @@ struct RecDesc {
 };
 
 // Lays out all records in precision S; fills the RecordSet's host images.
+// fixed (S = 4, short records only): the fixed layout of tri_kernel.cuh,
+// with ddst = -1 (no diagonal slot) and vdsrc = each value's row diagonal.
 void layout(const TriDeps& d, const std::vector<RecDesc>& recs, int S, std::vector<unsigned char>& buf,
             std::vector<long long>& off, std::vector<int>& nbytes, std::vector<long long>& vdst,
             std::vector<long long>& ddst, std::vector<long long>& idst,
             std::vector<int>* vsrc, std::vector<int>* dsrc, std::vector<int>* long_col,
-            std::vector<int>* long_src) {
+            std::vector<int>* long_src, bool fixed = false, std::vector<int>* vdsrc = nullptr) {
   buf.clear();
   off.clear();
   nbytes.clear();
@@ -73,6 +75,35 @@ void layout(const TriDeps& d, const std::vector<RecDesc>& recs, int S, std::vect
   idst.clear();
   for (const RecDesc& r : recs) {
     const int nrows = (int)r.rows.size();
+    if (fixed) {
+      const long long base = (long long)buf.size();
+      const long long bytes = kFixHdrBytes + (long long)kFixLaneBytes * nrows;
+      off.push_back(base);
+      nbytes.push_back((int)bytes);
+      buf.resize(base + bytes, 0);
+      int* hdr = reinterpret_cast<int*>(buf.data() + base);
+      hdr[0] = nrows;
+      hdr[1] = r.wait_for;
+      hdr[2] = (int)off.size() - 1;  // record index: the consumer checks the staged copy against it
+      hdr[3] = kFixTag;
+      for (int t = 0; t < nrows; ++t) {
+        const int row = r.rows[t];
+        const long long lb = base + kFixHdrBytes + (long long)kFixLaneBytes * t;
+        int* w = reinterpret_cast<int*>(buf.data() + lb);
+        w[0] = row;
+        for (int k = 0; k < kTriHeld; ++k) w[1 + k] = -1;
+        ddst.push_back(-1);
+        idst.push_back(lb / 4 + 1 + kTriHeld);
+        if (dsrc) dsrc->push_back(d.diag_src[row]);
+        for (int k = d.row_ptr[row], e = 0; k < d.row_ptr[row + 1]; ++k, ++e) {
+          w[1 + e] = d.dep_col[k];
+          vdst.push_back(lb / 4 + 2 + kTriHeld + e);
+          if (vsrc) vsrc->push_back(d.dep_src[k]);
+          if (vdsrc) vdsrc->push_back(d.diag_src[row]);
+        }
+      }
+      continue;
+    }
     const long long R4 = (nrows + 3) & ~3;
     const long long bytes = r.is_long ? rec_size(nrows, 0, S) : rec_size(nrows, r.len, S);
     const long long base = (long long)buf.size();
@@ -332,18 +363,24 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows, int level_run
   plan->ndiag = (int)dsrc.size();
   plan->nlong = (int)long_col.size();
   GB_TRY(upload_set(&plan->r64, buf, off, nbytes, vdst, ddst, idst, long_col.size(), 8));
-  {
-    // same record order, so the FP32 pass yields the same value/long order
-    std::vector<int> vs2, ds2, lc2, ls2;
-    layout(d, recs, 4, buf, off, nbytes, vdst, ddst, idst, &vs2, &ds2, &lc2, &ls2);
-  }
-  GB_TRY(upload_set(&plan->r32, buf, off, nbytes, vdst, ddst, idst, long_col.size(), 4));
-
   plan->short_only = true;
   for (const RecDesc& r : recs)
     if (r.is_long || r.len > kTriHeld) plan->short_only = false;
   if (const char* e = getenv("GBLAP_TRI_SHORT"))  // 0: always the general kernel
     if (e[0] == '0') plan->short_only = false;
+  // the FP32 records of a short-only plan in the fixed layout
+  // (GBLAP_TRI_FIXED=0: the general layout)
+  plan->fixed32 = plan->short_only;
+  if (const char* e = getenv("GBLAP_TRI_FIXED"))
+    if (e[0] == '0') plan->fixed32 = false;
+  {
+    // same record order, so the FP32 pass yields the same value/long order
+    std::vector<int> vs2, ds2, lc2, ls2, vds;
+    layout(d, recs, 4, buf, off, nbytes, vdst, ddst, idst, &vs2, &ds2, &lc2, &ls2, plan->fixed32,
+           plan->fixed32 ? &vds : nullptr);
+    if (plan->fixed32) GB_TRY(upload(&plan->vdsrc, vds));
+  }
+  GB_TRY(upload_set(&plan->r32, buf, off, nbytes, vdst, ddst, idst, long_col.size(), 4));
   plan->n = n;
   plan->lower = lower;
   plan->nlevels = nlev;
@@ -380,8 +417,8 @@ void tri_plan_free(TriPlan* p) {
   free_set(&p->r64);
   free_set(&p->r32);
   if (p->buf64s) cudaFree(p->buf64s);
-  void* ptrs[] = {p->tile_row0, p->tile_row1, p->tile_rec, p->rec_flags, p->vsrc, p->dsrc,
-                  p->long_col,  p->long_src,  p->order,    p->ticket,    p->part64, p->part32};
+  void* ptrs[] = {p->tile_row0, p->tile_row1, p->tile_rec, p->rec_flags, p->vsrc,   p->dsrc,  p->long_col,
+                  p->long_src,  p->order,     p->ticket,   p->part64,    p->part32, p->vdsrc};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   *p = TriPlan();
@@ -400,10 +437,30 @@ __global__ void fill_records_kernel(int nval, const long long* __restrict__ vdst
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nval; i += stride) buf[vdst[i]] = (T)ent[vsrc[i]];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ndiag; i += stride) {
     const double v = dg[dsrc[i]];
-    buf[ddst[i]] = (T)v;
+    if (ddst[i] >= 0) buf[ddst[i]] = (T)v;
     buf[idst[i]] = (T)(v != 0.0 ? 1.0 / v : 0.0);
   }
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nlong; i += stride) lval[i] = (T)ent[lsrc[i]];
+}
+
+// FP32 records in the fixed layout: the FMA form written directly -- each
+// entry times its row's reciprocal diagonal in FP64, rounded once (the same
+// values scale_records_kernel gives the general layout), and the
+// reciprocals.
+__global__ void fill_fixed32_kernel(int nval, const long long* __restrict__ vdst, const int* __restrict__ vsrc,
+                                    const int* __restrict__ vdsrc, const double* __restrict__ ent, int ndiag,
+                                    const long long* __restrict__ idst, const int* __restrict__ dsrc,
+                                    const double* __restrict__ dg, float* buf) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nval; i += stride) {
+    const double d = dg[vdsrc[i]];
+    const double dinv = d != 0.0 ? 1.0 / d : 0.0;
+    buf[vdst[i]] = (float)(ent[vsrc[i]] * dinv);
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ndiag; i += stride) {
+    const double d = dg[dsrc[i]];
+    buf[idst[i]] = (float)(d != 0.0 ? 1.0 / d : 0.0);
+  }
 }
 
 // FMA form: every short record's entry values times the reciprocal of their
@@ -456,10 +513,14 @@ int tri_plan_fill(TriPlan* p, const double* ent_src, const double* diag_src, int
                                                 (double*)p->r64.long_val);
   GB_CUDA_TRY(cudaGetLastError());
   if (mode == kFillFma32) {
-    fill_records_kernel<float><<<g, 256, 0, s>>>(p->nval, p->r32.vdst, p->vsrc, ent_src, p->ndiag,
-                                                 p->r32.ddst, p->r32.idst, p->dsrc, diag_src,
-                                                 p->nlong, p->long_src, (float*)p->r32.buf,
-                                                 (float*)p->r32.long_val);
+    if (p->fixed32)
+      fill_fixed32_kernel<<<g, 256, 0, s>>>(p->nval, p->r32.vdst, p->vsrc, p->vdsrc, ent_src, p->ndiag,
+                                            p->r32.idst, p->dsrc, diag_src, (float*)p->r32.buf);
+    else
+      fill_records_kernel<float><<<g, 256, 0, s>>>(p->nval, p->r32.vdst, p->vsrc, ent_src, p->ndiag,
+                                                   p->r32.ddst, p->r32.idst, p->dsrc, diag_src,
+                                                   p->nlong, p->long_src, (float*)p->r32.buf,
+                                                   (float*)p->r32.long_val);
     GB_CUDA_TRY(cudaGetLastError());
     p->have32 = true;
   }
@@ -467,11 +528,11 @@ int tri_plan_fill(TriPlan* p, const double* ent_src, const double* diag_src, int
     if (!p->buf64s) GB_CUDA_TRY(cudaMalloc(&p->buf64s, (size_t)p->r64.bytes));
     GB_CUDA_TRY(cudaMemcpyAsync(p->buf64s, p->r64.buf, (size_t)p->r64.bytes, cudaMemcpyDeviceToDevice, s));
   }
-  if (mode != kFillExact) {
+  if (mode != kFillExact && !(mode == kFillFma32 && p->fixed32)) {  // fixed FP32 records are written scaled
     if (p->nrec > 0) {
       const int gs = std::max(1, std::min(device_sm_count() * 8, ceil_div(p->nrec, 8)));
       scale_records_kernel<<<gs, 256, 0, s>>>(p->nrec, p->r64.off, p->r64.buf, p->r32.off,
-                                              mode == kFillFma32 ? p->r32.buf : nullptr,
+                                              mode == kFillFma32 && !p->fixed32 ? p->r32.buf : nullptr,
                                               mode == kFillFma64 ? p->buf64s : nullptr);
       GB_CUDA_TRY(cudaGetLastError());
     }
