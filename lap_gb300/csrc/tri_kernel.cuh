@@ -127,8 +127,9 @@ static_assert(kRecHdrBytes == 32, "record header layout");
 // issues all of its record's loads at once, with the header's beside them.
 constexpr int kFixHdrBytes = 16;
 constexpr int kFixLaneBytes = 48;
-// layout tag in the header: a record that lacks it is not read (the general
-// layout has a short record's entry offset, 0, in that word)
+// layout tag in the header, checked with the record index once a record is
+// solved (the general layout has a short record's entry offset, 0, there);
+// the launcher runs the fixed-layout kernel only on plans in that layout
 constexpr int kFixTag = 0x31584946;
 static_assert(kFixHdrBytes + 32 * kFixLaneBytes <= 2048, "a fixed record fits a ring slot");
 
@@ -401,12 +402,15 @@ struct RhsAhead {
 
 // The row a lane solves in a staged fixed-layout record (-1: idle lane).
 __device__ __forceinline__ int record_row_fixed(const unsigned char* rec, int lane) {
-  const int4 hd = *reinterpret_cast<const int4*>(rec);
+  const int nrows = *reinterpret_cast<const int*>(rec);
   const int row = *reinterpret_cast<const int*>(rec + kFixHdrBytes + lane * kFixLaneBytes);
-  return hd.w == kFixTag && lane < hd.x ? row : -1;
+  return lane < nrows ? row : -1;
 }
+// The index a staged record carries, or -1 for a fixed-layout kernel handed
+// a record without the layout's tag.
 __device__ __forceinline__ int record_index(const unsigned char* rec, bool fixed) {
-  return fixed ? reinterpret_cast<const int*>(rec)[2] : reinterpret_cast<const RecHdr*>(rec)->pad0;
+  const int* h = reinterpret_cast<const int*>(rec);
+  return fixed ? (h[3] == kFixTag ? h[2] : -1) : reinterpret_cast<const RecHdr*>(rec)->pad0;
 }
 
 // SHORT: the plan has only short records of at most kTriHeld dependencies
@@ -620,8 +624,7 @@ __device__ __forceinline__ void solve_record_fixed(const TriArgs<float>& A, OP& 
   const int4 hd = *reinterpret_cast<const int4*>(rec);
   const int4* lb = reinterpret_cast<const int4*>(rec + kFixHdrBytes + lane * kFixLaneBytes);
   const int4 b0 = lb[0], b1 = lb[1], b2 = lb[2];
-  if (hd.w != kFixTag && lane == 0) atomicCAS(A.err, 0, (int)GB_INTERNAL);
-  const bool act = hd.w == kFixTag && lane < hd.x;
+  const bool act = lane < hd.x;
   const int row = b0.x;
   typename OP::Pre pr;
   typename OP::DPre dp;
