@@ -49,6 +49,11 @@ __device__ __forceinline__ void ep_prefetch(EP&, int, long) {}
 // Values of a row held in registers from the start of its bundle (FMA
 // form): a stencil row's whole dependency list is in flight at once.
 constexpr int kSpmvHeld = 8;
+// 1: bundles whose rows all have at most kSpmvHeld entries take the
+// per-lane form (no staging).
+#ifndef GB_SPMV_SHORT_ROWS
+#define GB_SPMV_SHORT_ROWS 1
+#endif
 // 1: the FMA form stages the matrix values beside the gathered x (coalesced
 // loads; the row sums then read shared memory only), in bundles of half the
 // entries so the staging takes the same shared memory.
@@ -63,7 +68,7 @@ constexpr int kSpmvHeld = 8;
 // Latency structure of a bundle: its row bounds (one coalesced load per
 // lane) -> the column indices (coalesced over the bundle's entries) and, in
 // the FMA form, the row's first kSpmvHeld values -> the x gathers -> the row
-// sums.  init() and the epilogue's loads are issued with the row bounds.
+// sums.  The epilogue's loads are issued before the row bounds.
 template <typename T, bool EXACT, typename XF, typename EP>
 __device__ __forceinline__ void spmv_bundle(int b, int n, const int* __restrict__ bundles,
                                             const int* __restrict__ ia,
@@ -82,6 +87,9 @@ __device__ __forceinline__ void spmv_bundle(int b, int n, const int* __restrict_
   const int nr = r1 - r0;
   const int r = r0 + lane;
   const bool own = lane < nr;
+  // the epilogue's loads first: they do not depend on the row bounds (a
+  // row of the long-row path below issues them again, in lane 0)
+  if (own) ep_prefetch(ep, r, 0);
   // this lane's row bounds; lane nr-1's end is the bundle's
   const int rs = own ? __ldg(ia + r) : 0;
   const int re = own ? __ldg(ia + r + 1) : 0;
@@ -104,10 +112,36 @@ __device__ __forceinline__ void spmv_bundle(int b, int n, const int* __restrict_
     __syncwarp();
     return;
   }
+#if GB_SPMV_SHORT_ROWS
+  // Every row of the bundle has at most kSpmvHeld entries (stencils): each
+  // lane loads its own row's columns and values and gathers its x values,
+  // all of them in flight at once -- no staging pass.  The same FMA chain,
+  // in the same order, as the staged form below.
+  if (!EXACT && __all_sync(0xffffffffu, !own || re - rs <= kSpmvHeld)) {
+    if (own) {
+      T acc = ep.init(r);
+      int c[kSpmvHeld];
+      T av[kSpmvHeld], xv[kSpmvHeld];
+#pragma unroll
+      for (int u = 0; u < kSpmvHeld; ++u) {
+        const bool in = rs + u < re;
+        c[u] = in ? __ldg(ja + rs + u) : -1;
+        av[u] = in ? __ldg(a + rs + u) : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < kSpmvHeld; ++u) xv[u] = c[u] >= 0 ? xf(c[u]) : T(0);
+#pragma unroll
+      for (int u = 0; u < kSpmvHeld; ++u)
+        if (c[u] >= 0) acc = fma_rn(av[u], xv[u], acc);
+      ep.store(r, acc);
+    }
+    __syncwarp();
+    return;
+  }
+#endif
   T acc = T(0);
   T held[kSpmvHeld];
   if (own) {
-    ep_prefetch(ep, r, 0);
     acc = ep.init(r);
     if (!EXACT && !GB_SPMV_STAGE_A) {
 #pragma unroll
