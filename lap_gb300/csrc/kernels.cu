@@ -85,6 +85,15 @@ int spmv_plan_build(int n, int nnz, const int* ia, SpmvPlan* plan, int rpb) {
   plan->nbundles = (int)b.size() - 1;
   plan->long_rows = longs;
   plan->rows_per_bundle = rpb;
+  // every bundle 32 consecutive rows (a stencil): the kernels' plan-free
+  // layout computes the same bundles, one dependent load fewer per bundle
+  bool uniform = rpb == kBundleRows && longs == 0;
+  for (size_t i = 0; uniform && i + 1 < b.size(); ++i)
+    if (b[i] != (int)(i * kBundleRows)) uniform = false;
+  if (uniform) {
+    plan->bundles = nullptr;
+    return GB_OK;
+  }
   GB_CUDA_TRY(cudaMalloc(&plan->bundles, sizeof(int) * b.size()));
   GB_CUDA_TRY(cudaMemcpy(plan->bundles, b.data(), sizeof(int) * b.size(), cudaMemcpyHostToDevice));
   return GB_OK;

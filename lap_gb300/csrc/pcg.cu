@@ -177,7 +177,8 @@ __global__ void __launch_bounds__(kThreads)
 // ------------------------------------------------------------ update
 template <typename T, int WK>
 __global__ void __launch_bounds__(kThreads)
-    update_kernel(int n, T* x, T* r, T* w, const T* __restrict__ p, const T* __restrict__ q,
+    update_kernel(int n, T* __restrict__ x, T* __restrict__ r, T* __restrict__ w, const T* __restrict__ p,
+                  const T* __restrict__ q,
                   const T* __restrict__ d_r, PcgState* st, double* part, double* hist,
                   cudaGraphConditionalHandle cond, int has_cond) {
   __shared__ double sm[2 * kThreads / 32];
