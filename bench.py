@@ -364,6 +364,12 @@ def run_workload(args, local):
             line[f"precision{p}"] = {"ms": round(r["device_ms"], 2), "iters": r["iters"], "outer": r["outer"],
                                      "flag": r["flag"], "rel_true_res": r["rel_true_res"],
                                      "rel_err_vs_fp64": float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64))}
+        # the mode chosen by timing (gb_pcg_autotune_precision), then a solve in it
+        tune = sysm.autotune_precision(db, **kw)
+        x, r = sysm.solve(db, precision=-1, **kw)
+        line["autotune_precision"] = {"best": tune["best"], "ms_per_mode": [round(v, 2) for v in tune["ms"]],
+                                      "solve_ms": round(r["device_ms"], 2), "iters": r["iters"],
+                                      "rel_err_vs_fp64": float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64))}
     elif wl == "batch512":
         mats, rhs = gen.knn_batch(512, seed=1004)
         line["config"] = (f"512 kNN(k=8) Laplacians, n log-uniform 1k-200k (sum n = {sum(A.n for A in mats)}, "

@@ -102,7 +102,10 @@ typedef struct {
                            inside FP64 iterative refinement.
                         2: split: FP64 Krylov vectors and scalars around an FP32 SpMV and
                            FP32 triangular-solve preconditioner ("ichol", "GS_std" with
-                           k = 1), with FP64 residual replacement.  */
+                           k = 1), with FP64 residual replacement.
+                        -1 (gb_pcg_solve, gb_pcg_solve_host): the mode
+                           gb_pcg_autotune_precision chose for the system (0 until it
+                           has run).  */
   double inner_tol;  /* mixed: residual reduction between refinement / replacement steps;
                         0 (default) selects 1e-4 for precision 1 and 1e-2 for precision 2.
                         A cycle never runs past the solve's own tolerance. */
@@ -219,6 +222,16 @@ int gb_batch_autotune(gb_batch batch, const double *b, int iters, int *rows_per_
  * per (n, nnz, nrhs)).  No counterpart in LAP. */
 int gb_pcg_autotune_multi(gb_system sys, int nrhs, const double *B, int iters, int *width, double *ms_default,
                           double *ms_best);
+
+/* Picks the precision mode of the system's solves by timing: one solve of b
+ * (device, x0 = 0) with *opts in each mode 0, 1, 2 that the system supports,
+ * each timed on its second run (the first also captures the mode's graph and
+ * fills its FP32 records).  The fastest that converged is kept on the system
+ * (used by precision = -1) and returned in *best; ms_host[3] (may be NULL)
+ * receives each mode's device time, -1 where the mode is unsupported or did
+ * not converge.  GB_MAXIT when no mode converged.  No counterpart in LAP. */
+int gb_pcg_autotune_precision(gb_system sys, const double *b, const gb_pcg_opts *opts, int *best,
+                              double *ms_host);
 
 /* ------------------------------------------------------------ failure injection */
 /* Test hook: wall-clock limit (ns) of every sync-free wait in this system's

@@ -106,6 +106,7 @@ def _proto(L: C.CDLL) -> None:
         "gb_autotune_spmv": (i, [vp, C.POINTER(i)]),
         "gb_batch_autotune": (i, [vp, vp, i, C.POINTER(i), C.POINTER(i), C.POINTER(d), C.POINTER(d)]),
         "gb_pcg_autotune_multi": (i, [vp, i, vp, i, C.POINTER(i), C.POINTER(d), C.POINTER(d)]),
+        "gb_pcg_autotune_precision": (i, [vp, vp, vp, C.POINTER(i), vp]),
         "gb_debug_set_spin_budget": (i, [vp, C.c_ulonglong]),
         "gb_dot_noalloc": (i, [i, vp, vp, C.POINTER(C.c_double), vp]),
         "gb_mm_read_csr": (i, [C.c_char_p, C.POINTER(MmCsr)]),
@@ -242,6 +243,20 @@ class System:
         if hist_len:
             return x, out, hist[: min(hist_len, r.iters + 1)]
         return x, out
+
+    def autotune_precision(self, b, **kw) -> dict:
+        """gb_pcg_autotune_precision: the fastest converging precision mode
+        for b, kept on the system (solve(..., precision=-1) uses it)."""
+        import torch
+
+        b = b.to(device="cuda", dtype=torch.float64).contiguous()
+        o = opts(**kw)
+        best = C.c_int(-1)
+        ms = np.zeros(3)
+        torch.cuda.synchronize()
+        check(lib().gb_pcg_autotune_precision(self.h, ptr(b), C.byref(o), C.byref(best), ms.ctypes.data),
+              "gb_pcg_autotune_precision")
+        return dict(best=best.value, ms=[float(v) for v in ms])
 
     def solve_host(self, b: np.ndarray, x0: np.ndarray | None = None, **kw):
         """Same solve from/to host numpy arrays (copies inside the call)."""

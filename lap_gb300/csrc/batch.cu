@@ -567,7 +567,9 @@ __global__ void __launch_bounds__(kBatchThreads)
   double a0 = 0.0, a1 = 0.0, a2 = 0.0;
   if (__any_sync(0xffffffffu, live || rep)) {
     for (int bb = L.w0; bb < B.nbun; bb += L.W) {
-      const int r0 = __ldg(B.bundles + bb), r1 = __ldg(B.bundles + bb + 1);
+      // a system plan of uniform 32-row bundles has no table (plan-free layout)
+      const int r0 = B.bundles ? __ldg(B.bundles + bb) : bb * kBundleRows;
+      const int r1 = B.bundles ? __ldg(B.bundles + bb + 1) : min(r0 + kBundleRows, B.n1);
       bool wide = false;
       if (lane < r1 - r0) {
         const int row = r0 + lane, k0 = __ldg(B.ia + row), k1 = __ldg(B.ia + row + 1);

@@ -86,7 +86,8 @@ int spmv_plan_build(int n, int nnz, const int* ia, SpmvPlan* plan, int rpb) {
   plan->long_rows = longs;
   plan->rows_per_bundle = rpb;
   // every bundle 32 consecutive rows (a stencil): the kernels' plan-free
-  // layout computes the same bundles, one dependent load fewer per bundle
+  // layout computes the same bundles, one dependent load fewer per bundle.
+  // Every reader of SpmvPlan::bundles takes nullptr as that layout.
   bool uniform = rpb == kBundleRows && longs == 0;
   for (size_t i = 0; uniform && i + 1 < b.size(); ++i)
     if (b[i] != (int)(i * kBundleRows)) uniform = false;

@@ -619,8 +619,11 @@ static int read_state(gb_system s, PcgState* dst, const PcgState* src) {
 }
 
 // Core solve on the internal buffers b_int (rhs) and v64.x (x0 -> x).
-static int solve_internal(gb_system s, const gb_pcg_opts* o, gb_pcg_result* res, double* hist_host,
+static int solve_internal(gb_system s, const gb_pcg_opts* oin, gb_pcg_result* res, double* hist_host,
                           int hist_len) {
+  gb_pcg_opts oc = *oin;
+  if (oc.precision < 0) oc.precision = s->auto_precision;  // the autotuner's choice
+  const gb_pcg_opts* o = &oc;
   GB_TRY(system_ensure_hist(s, o->maxit));
   GB_CUDA_TRY(cudaMemsetAsync(s->err, 0, sizeof(int), s->s));
   gb_pcg_result r;
@@ -853,4 +856,49 @@ extern "C" int gb_ichol_factor_values(gb_system s, double* l_vals, double* u_val
   if (u_vals) GB_TRY(gather_values(s->lu_len, s->lower_row, s->fac, u_vals, nullptr, s->s));
   GB_CUDA_TRY(cudaStreamSynchronize(s->s));
   return s->zero_pivot_row ? GB_ZERO_PIVOT : GB_OK;
+}
+
+extern "C" int gb_pcg_autotune_precision(gb_system s, const double* b, const gb_pcg_opts* opts, int* best,
+                                         double* ms_host) {
+  if (!s || !b) return GB_BAD_INPUT;
+  gb_pcg_opts o;
+  if (opts) o = *opts;
+  else gb_pcg_opts_default(&o);
+  double* x = nullptr;
+  GB_CUDA_TRY(cudaMalloc(&x, sizeof(double) * s->n));
+  int pick = -1, rc = GB_OK;
+  double pick_ms = 0.0;
+  for (int p = 0; p < 3 && rc == GB_OK; ++p) {
+    o.precision = p;
+    double t = -1.0;
+    for (int rep = 0; rep < 2; ++rep) {
+      if (cudaMemsetAsync(x, 0, sizeof(double) * s->n, s->s) != cudaSuccess) {
+        rc = GB_CUDA_ERROR;
+        break;
+      }
+      gb_pcg_result r;
+      const int st = gb_pcg_solve(s, b, x, &o, nullptr, 0, &r);
+      if (st == GB_NOT_SUPPORTED) {  // a mode this preconditioner has not
+        t = -1.0;
+        break;
+      }
+      if (st != GB_OK) {
+        rc = st;
+        break;
+      }
+      t = (r.status == GB_OK && r.flag == 0) ? r.device_ms : -1.0;
+      if (t < 0.0) break;  // did not converge
+    }
+    if (ms_host) ms_host[p] = t;
+    if (t >= 0.0 && (pick < 0 || t < pick_ms)) {
+      pick = p;
+      pick_ms = t;
+    }
+  }
+  cudaFree(x);
+  if (rc != GB_OK) return rc;
+  if (pick < 0) return GB_MAXIT;
+  s->auto_precision = pick;
+  if (best) *best = pick;
+  return GB_OK;
 }

@@ -77,6 +77,7 @@ struct gb_system_s {
   double *aux1 = nullptr, *aux2 = nullptr, *aux3 = nullptr;
   double* part = nullptr;
   int part_len = 0;
+  int auto_precision = 0;  // the mode gb_pcg_autotune_precision chose (gb_pcg_opts precision -1)
   gb::PcgState* st = nullptr;      // FP64 recurrence (or the inner FP32 one)
   gb::PcgState* st_out = nullptr;  // outer refinement state
   gb::PcgState* st_host = nullptr; // pinned staging
