@@ -366,9 +366,12 @@ def run_workload(args, local):
                                      "rel_err_vs_fp64": float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64))}
         # the mode chosen by timing (gb_pcg_autotune_precision), then a solve in it
         tune = sysm.autotune_precision(db, **kw)
-        x, r = sysm.solve(db, precision=-1, **kw)
+        sysm.solve(db, precision=-1, **kw)
+        res = _timed_solves(lambda: sysm.solve(db, precision=-1, **kw), 3)
+        x, r = res[-1]
         line["autotune_precision"] = {"best": tune["best"], "ms_per_mode": [round(v, 2) for v in tune["ms"]],
-                                      "solve_ms": round(r["device_ms"], 2), "iters": r["iters"],
+                                      "solve_ms": round(statistics.mean(rr["device_ms"] for _, rr in res), 2),
+                                      "iters": r["iters"],
                                       "rel_err_vs_fp64": float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64))}
     elif wl == "batch512":
         mats, rhs = gen.knn_batch(512, seed=1004)

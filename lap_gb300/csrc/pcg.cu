@@ -126,8 +126,11 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------------ spmv_pq
+// Five resident blocks per SM, as spmv_pq_split_kernel: the FP64 form then
+// holds 48 registers with a 72-byte spill instead of 64 (128^3: 69.0 ->
+// 62.4 us); the FP32 form needs 48 either way.
 template <typename T, int WK>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 5)
     spmv_pq_kernel(int n, int nb, const int* __restrict__ bundles, const int* __restrict__ ia,
                    const int* __restrict__ ja, const T* __restrict__ a, const T* __restrict__ w,
                    T* p, T* q, T* tfill, PcgState* st, double* part,
@@ -392,7 +395,10 @@ __global__ void __launch_bounds__(kThreads)
 // Split precision: q = A w + beta q and p = w + beta p with w the FP32 output
 // of the preconditioner, A's FP32 values and FP32 products (A w), and p, q,
 // beta and p'q in FP64.  By linearity q = A p as in spmv_pq_kernel.
-__global__ void __launch_bounds__(kThreads)
+// Five resident blocks per SM (at most 51 registers, no spills; 64 without
+// the bound): this latency-bound kernel needs the warps (128^3: 48.3 ->
+// 45.6 us; six or eight blocks spill and measured 48.1 / 53.1 us).
+__global__ void __launch_bounds__(kThreads, 5)
     spmv_pq_split_kernel(int n, int nb, const int* __restrict__ bundles, const int* __restrict__ ia,
                          const int* __restrict__ ja, const float* __restrict__ a,
                          const float* __restrict__ w, double* p, double* q, float* tfill,
