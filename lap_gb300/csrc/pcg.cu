@@ -438,8 +438,11 @@ __global__ void __launch_bounds__(kThreads, 5)
     }
   } ep{w, p, q, tfill, beta, first, 0.0, 0.0f, 0.0, 0.0};
   const int wid = threadIdx.x >> 5;
-  for (int bb = blockIdx.x * (kThreads / 32) + wid; bb < nb; bb += gridDim.x * (kThreads / 32))
-    spmv_bundle<float, false>(bb, n, bundles, ia, ja, a, 1.0f, xf, ep, stage[wid]);
+  // each bundle's head loaded while the previous bundle is worked on (128^3:
+  // 45.9 -> 44.7 us; the FP64 kernel, which then spills more, measured
+  // slower with it: 62.1 -> 68 us)
+  spmv_bundles<float, false>(blockIdx.x * (kThreads / 32) + wid, gridDim.x * (kThreads / 32), nb, n, bundles, ia, ja,
+                             a, 1.0f, xf, ep, stage[wid]);
   double acc[1] = {ep.pq};
   if (reduce_last<1>(acc, part, gridDim.x, blockIdx.x, &st->tk[TK_PQ], sm) && threadIdx.x == 0)
     st->pq = acc[0];

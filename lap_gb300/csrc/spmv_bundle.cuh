@@ -69,21 +69,36 @@ constexpr int kSpmvHeld = 8;
 // lane) -> the column indices (coalesced over the bundle's entries) and, in
 // the FMA form, the row's first kSpmvHeld values -> the x gathers -> the row
 // sums.  The epilogue's loads are issued before the row bounds.
-template <typename T, bool EXACT, typename XF, typename EP>
-__device__ __forceinline__ void spmv_bundle(int b, int n, const int* __restrict__ bundles,
-                                            const int* __restrict__ ia,
-                                            const int* __restrict__ ja,
-                                            const T* __restrict__ a, T alpha, XF& xf, EP& ep,
-                                            T* stage) {
-  const int lane = threadIdx.x & 31;
-  int r0, r1;
+// The head of bundle b: its rows [r0, r1) and this lane's row bounds
+// [rs, re) -- the loads a bundle's chain starts with.  The grid-stride loops
+// load the next bundle's head before they work on the current one
+// (spmv_bundles), so that round trip overlaps the bundle in hand.
+struct BundleHead {
+  int r0, r1, rs, re;
+};
+__device__ __forceinline__ BundleHead bundle_head(int b, int n, const int* __restrict__ bundles,
+                                                  const int* __restrict__ ia) {
+  BundleHead h;
   if (bundles) {
-    r0 = __ldg(bundles + b);
-    r1 = __ldg(bundles + b + 1);
+    h.r0 = __ldg(bundles + b);
+    h.r1 = __ldg(bundles + b + 1);
   } else {
-    r0 = b * 32;
-    r1 = min(r0 + 32, n);
+    h.r0 = b * 32;
+    h.r1 = min(h.r0 + 32, n);
   }
+  const int lane = threadIdx.x & 31;
+  const bool own = lane < h.r1 - h.r0;
+  h.rs = own ? __ldg(ia + h.r0 + lane) : 0;
+  h.re = own ? __ldg(ia + h.r0 + lane + 1) : 0;
+  return h;
+}
+
+template <typename T, bool EXACT, typename XF, typename EP>
+__device__ __forceinline__ void spmv_bundle_h(const BundleHead& h, const int* __restrict__ ia,
+                                              const int* __restrict__ ja, const T* __restrict__ a, T alpha, XF& xf,
+                                              EP& ep, T* stage) {
+  const int lane = threadIdx.x & 31;
+  const int r0 = h.r0, r1 = h.r1;
   const int nr = r1 - r0;
   const int r = r0 + lane;
   const bool own = lane < nr;
@@ -91,8 +106,8 @@ __device__ __forceinline__ void spmv_bundle(int b, int n, const int* __restrict_
   // row of the long-row path below issues them again, in lane 0)
   if (own) ep_prefetch(ep, r, 0);
   // this lane's row bounds; lane nr-1's end is the bundle's
-  const int rs = own ? __ldg(ia + r) : 0;
-  const int re = own ? __ldg(ia + r + 1) : 0;
+  const int rs = h.rs;
+  const int re = h.re;
   const int j0 = __shfl_sync(0xffffffffu, rs, 0);
   const int j1 = __shfl_sync(0xffffffffu, re, nr - 1);
   if (j1 - j0 > (GB_SPMV_STAGE_A && !EXACT ? kBundleNnz / 2 : kBundleNnz)) {
@@ -185,6 +200,29 @@ __device__ __forceinline__ void spmv_bundle(int b, int n, const int* __restrict_
     ep.store(r, acc);
   }
   __syncwarp();
+}
+
+template <typename T, bool EXACT, typename XF, typename EP>
+__device__ __forceinline__ void spmv_bundle(int b, int n, const int* __restrict__ bundles,
+                                            const int* __restrict__ ia, const int* __restrict__ ja,
+                                            const T* __restrict__ a, T alpha, XF& xf, EP& ep, T* stage) {
+  spmv_bundle_h<T, EXACT>(bundle_head(b, n, bundles, ia), ia, ja, a, alpha, xf, ep, stage);
+}
+
+// Bundles b0, b0 + step, ... < nb, each bundle's head loaded while the one
+// before it is worked on.
+template <typename T, bool EXACT, typename XF, typename EP>
+__device__ __forceinline__ void spmv_bundles(int b0, int step, int nb, int n, const int* __restrict__ bundles,
+                                             const int* __restrict__ ia, const int* __restrict__ ja,
+                                             const T* __restrict__ a, T alpha, XF& xf, EP& ep, T* stage) {
+  if (b0 >= nb) return;
+  BundleHead h = bundle_head(b0, n, bundles, ia);
+  for (int b = b0; b < nb; b += step) {
+    const int bn = b + step;
+    const BundleHead hn = bn < nb ? bundle_head(bn, n, bundles, ia) : h;
+    spmv_bundle_h<T, EXACT>(h, ia, ja, a, alpha, xf, ep, stage);
+    h = hn;
+  }
 }
 
 // Simple x functor: x[col].
