@@ -313,6 +313,11 @@ struct OpSplitLower {
 // IC(0) upper solve: y = U^{-1} t only; r'w follows in rho_kernel.
 template <typename T>
 struct OpSplitUpper {
+  // FP32 upper solves poll values (one loop over a lane's pending ones),
+  // on plane tiles in pushing clusters like the lower: 128^3 upper 267 ->
+  // 250 us.  On two-plane tiles in pulling clusters polling changed
+  // nothing, and FP64 upper solves measured slower polling.
+  static constexpr bool kPollValues = sizeof(T) == 4;
   const T* t;
   PcgState* st;
   bool dn;

@@ -315,7 +315,10 @@ extern "C" int gb_system_create(int n, int nnz, const int* ia, const int* ja, co
     // GBLAP_TRI_TILE_ROWS32 sets both explicitly.
     const bool t32_env = getenv("GBLAP_TRI_TILE_ROWS32") != nullptr;
     const int t32l = t32_env ? tri_default_tile_rows32(n) : tri_default_tile_rows(n);
-    const int t32u = tri_default_tile_rows32(n);
+    // FP32 upper tiles as the lower ones: their solves poll values too
+    // (OpSplitUpper<float>), which pays on plane tiles (128^3: 250 us
+    // against 267 on two-plane tiles)
+    const int t32u = t32l;
     // The four plans are independent host work (levels, record packing,
     // layout): built on parallel threads, each with this thread's device
     // current (4.19M-row Chung-Lu: 8.8 s one after another).
