@@ -13,14 +13,20 @@
 // inside a tile rows are ordered by their global level (dependency depth in
 // the whole factor) and packed into RECORDS of at most 32 rows of one level (rows,
 // diagonal, its reciprocal, dependency columns and values column-major;
-// contiguous and 16-byte aligned).  One CTA solves one tile at a time:
+// contiguous and 16-byte aligned).  The FP32 records of a plan whose rows all
+// have at most kTriHeld dependencies use a fixed layout instead (one 48-byte
+// block per row at a fixed offset), read by the short-record kernel only.
+// One CTA solves one tile at a time:
 //   * a producer warp streams the tile's records into a ring of shared-
 //     memory slots with cp.async.bulk (TMA), one mbarrier per slot, several
 //     lanes issuing copies in parallel;
 //   * consumer warps take the records round-robin, one row per lane.  A
 //     dependency inside the tile is read from the tile's solution array in
-//     shared memory, spinning while it still holds the sentinel; one in an
-//     earlier tile is read from global memory the same way, with backoff.
+//     shared memory, spinning while it still holds the sentinel (or, in the
+//     counter form, once the tile's earlier levels are counted complete);
+//     one in an earlier tile is read from the inbox the previous tile's CTA
+//     pushes into, from that CTA's array, or from global memory with
+//     backoff, by the launch form.
 //     There is no barrier between levels: a row waits exactly for its own
 //     dependencies, so the wavefront advances at shared-memory latency.
 //     A row's right-hand side is loaded before its dependencies are awaited.
