@@ -339,6 +339,31 @@ def test_cluster_form_matches_per_cta_form(tmp_path):
                 assert np.array_equal(a, c), (prec, p, cl)
 
 
+def test_fixed_record_layout_matches_general_layout(tmp_path):
+    """The FP32 records of a short-only plan are kept in the fixed layout
+    (one 48-byte block per row, read by the short-record kernel); with
+    GBLAP_TRI_FIXED=0 they keep the general layout and run the general
+    kernel.  Each row's terms are folded in the same order in both, so the
+    FP32-Krylov and split solutions must be bitwise identical."""
+    import os
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = {}
+    for fixed in ("1", "0"):
+        env = dict(os.environ, GBLAP_TRI_FIXED=fixed)
+        stem = str(tmp_path / f"fx{fixed}")
+        subprocess.run([sys.executable, "-c", _CLUSTER_CHILD, root, stem], env=env, check=True,
+                       timeout=600)
+        out[fixed] = stem
+    for prec in ("ichol", "GS_std"):
+        for p in (1, 2):
+            a = np.load(f"{out['1']}_{prec}_{p}.npy")
+            c = np.load(f"{out['0']}_{prec}_{p}.npy")
+            assert np.array_equal(a, c), (prec, p)
+
+
 _LEVELS_CHILD = r"""
 import sys, json, ctypes as C, numpy as np, torch
 sys.path.insert(0, sys.argv[1])
