@@ -40,7 +40,7 @@ int tri_plan_build(const TriDeps& d, TriPlan* plan, int tile_rows = 0, int level
 // consumer warps of one triangular-solve CTA for elements of elem_bytes
 int tri_consumer_warps(int elem_bytes);
 int tri_default_tile_rows(int n);
-// Tile rows of the FP32-only plans: twice the FP64 default (32768 at most).
+// Tile rows of the FP32 plans: the FP64 default, or GBLAP_TRI_TILE_ROWS32.
 int tri_default_tile_rows32(int n);
 // Resident CTAs per SM of the tiled solves (default 1, limited by shared
 // memory anyway); GBLAP_TRI_BLOCKS_PER_SM overrides it (1..8).

@@ -308,16 +308,12 @@ extern "C" int gb_system_create(int n, int nnz, const int* ia, const int* ja, co
       CKC(cudaMemset(s->fac_ticket, 0, sizeof(unsigned) * 4));
     }
     ph.mark("dependency lists");
-    // FP32 tiles: the lower factor's as tall as the FP64 ones, which leaves
-    // shared memory for the inbox of the pushing cluster form; the upper
-    // factor's twice that, solved in pulling clusters (on 128^3: lower 284
-    // vs 473 us, upper 374 vs 335 us per split solve, measured both ways).
+    // FP32 tiles of both factors as tall as the FP64 ones, which leaves
+    // shared memory for the inbox of the pushing cluster form; both FP32
+    // solves poll values there (128^3 split solve: lower 284 vs 473 us on
+    // twice-as-tall tiles in pulling clusters; upper 250 vs 267 us).
     // GBLAP_TRI_TILE_ROWS32 sets both explicitly.
-    const bool t32_env = getenv("GBLAP_TRI_TILE_ROWS32") != nullptr;
-    const int t32l = t32_env ? tri_default_tile_rows32(n) : tri_default_tile_rows(n);
-    // FP32 upper tiles as the lower ones: their solves poll values too
-    // (OpSplitUpper<float>), which pays on plane tiles (128^3: 250 us
-    // against 267 on two-plane tiles)
+    const int t32l = tri_default_tile_rows32(n);
     const int t32u = t32l;
     // The four plans are independent host work (levels, record packing,
     // layout): built on parallel threads, each with this thread's device

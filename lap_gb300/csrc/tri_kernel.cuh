@@ -1127,8 +1127,8 @@ int tri_launch_short(const TriPlan& p, const TriArgs<T>& A, OP op, cudaStream_t 
     return fixed ? tri_launch_cl<T, OP, EXACT, 1, false, POLL, true>(p, A, op, s, smem) : GB_NOT_SUPPORTED;
   // FP32: clusters of 16 when every group is resident at once, else of 10
   // when that makes them all resident (two fit on most GPCs), else of 16.
-  // 128^3: the 64 upper tiles run in 16s; the 128 lower plane tiles in 10s
-  // (249 vs 257 us; 8 / 12 measured 254 / 280).
+  // 128^3: the 128 plane tiles of either factor run in 10s (lower 249 vs
+  // 257 us in 16s; 8 / 12 measured 254 / 280).
   if constexpr (sizeof(T) == 4) {
     if (smem_inbox <= (size_t)kTriMaxDynSmem) {
       int rc = tri_launch_cl<T, OP, EXACT, 16, false, POLL, true>(p, A, op, s, smem_inbox, true);

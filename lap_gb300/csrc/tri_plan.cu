@@ -499,9 +499,8 @@ int tri_default_tile_rows32(int n) {
     const int v = atoi(e);
     if (v >= 32 && v <= kTriMaxTileRows32) return v;
   }
-  // FP32 values take half the shared memory: twice the FP64 tile, so a
-  // dependency chain crosses half as many tile boundaries
-  return std::min(kTriMaxTileRows32, 2 * tri_default_tile_rows(n));
+  // as the FP64 tile: half the shared memory, the other half for the inbox
+  return tri_default_tile_rows(n);
 }
 
 int tri_plan_fill(TriPlan* p, const double* ent_src, const double* diag_src, int mode,
