@@ -593,7 +593,12 @@ def run_ours(args, world, rank, local):
     # spmv_pq_split, update, lower, upper), an outer residual after each of the
     # `outer` pauses, 4 per resume (resume, fill, lower, upper; all pauses but
     # the last), final true residual 1
-    launches_mixed = 1 + 4 + 4 * it_in + outer + 4 * max(outer - 1, 0) + 1
+    # our kernels per split solve: the first FP64 residual; the prologue
+    # (residual, sentinel fill, the two triangular solves, r'w); 5 per
+    # iteration (SpMV, update, the two solves, r'w); per replacement its
+    # FP64 residual and, unless it ends the solve, the resume (state reset,
+    # sentinel fill, solves, r'w); the final true residual
+    launches_mixed = 1 + 5 + 5 * it_in + outer + 5 * max(outer - 1, 0) + 1
     line = {"metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v, 4),
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
