@@ -76,14 +76,15 @@ namespace gb {
 #ifndef GB_TRI_RHS_AHEAD
 #define GB_TRI_RHS_AHEAD 1
 #endif
-// The short-record kernel (SHORT below) has its own counts.  FP32: 15 as
-// well (23 and 31 warps, at 85 and 64 registers without spills, measured
-// slower on the 128^3 IC(0) solves: lower 285 / 306 us against 257).
+// The short-record kernel (SHORT below) has its own counts.  FP32: 13 (128^3
+// split PCG with the fixed-layout records and polling solves: 119.8 ms
+// against 121.0 with 15 and 123.0 with 17; 11, 19, 23 and 31 measured slower
+// earlier).
 // FP64: 12 (128^3 FP64 lower / upper 298 / 339 us; 8 warps 321 / 364, 15
 // warps 308 / 340): its records are short enough that more warps in flight
 // outweigh the queueing on the FP64 pipe.
 #ifndef GB_TRI_CONSUMERS32S
-#define GB_TRI_CONSUMERS32S GB_TRI_CONSUMERS32
+#define GB_TRI_CONSUMERS32S 13
 #endif
 #ifndef GB_TRI_CONSUMERS64S
 #define GB_TRI_CONSUMERS64S 12
