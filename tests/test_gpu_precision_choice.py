@@ -3,14 +3,17 @@ mode's converged solve, and precision = -1 solving in that mode."""
 import numpy as np
 import pytest
 
-import lap_gb300 as gb
-from lap_gb300 import gen
-
 pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a GPU", allow_module_level=True)
+
+import lap_gb300 as gb  # noqa: E402
+from lap_gb300 import gen  # noqa: E402
 
 
 def _system(prec, n=24):
-    import torch
     A, b = gen.grid3d_lognormal(n, seed=1002)
     return gb.System.from_csr(A, prec), torch.from_numpy(b).cuda()
 
